@@ -1,0 +1,127 @@
+// Shared device-side definitions of the GB300 EOB pipeline: per-binary
+// record, status bits, and the workspace layout carved out of one
+// caller-provided device buffer (the library never allocates).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include "physics/fac_coeffs.h"
+#include "physics/ham_coeffs.h"
+#include "physics/ham_eval.h"
+#include "physics/flux_eval.h"
+#include "physics/mode_eval.h"
+#include "../../include/eobgb300.h"
+
+namespace eob {
+
+// Everything the integrator needs for one binary (built once by the setup
+// kernel; read-only afterwards).
+struct BinaryRec {
+    HamCoeffs ham;
+    FluxTable flux;
+    double pre_re[kNumLM], pre_im[kNumLM];
+    double m1s, m2s, chi1, chi2, Mt, omega0, nu;
+    double y0[4];      // initial state (r0, 0, pr0, pphi0)
+    int ic_iters, pad;
+};
+
+constexpr int kMaxModes = 5;
+constexpr int kChunk = 1024;   // samples per synthesis work item
+constexpr int kTrajStride = 5; // t, r, phi, pr, pphi per trajectory row
+
+struct WsLayout {
+    size_t bins, fac, traj, nsteps, status, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, total;
+    int Bc, Lc, Kc, Nc, nsubs, max_chunks;
+};
+
+EOB_HD size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Offsets of every array inside the workspace for capacities (Bc binaries,
+// Lc trajectory rows per binary, Kc modes, Nc samples).
+EOB_HD WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
+{
+    WsLayout w;
+    w.Bc = Bc; w.Lc = Lc; w.Kc = Kc; w.Nc = Nc;
+    w.nsubs = 1 + 2 * Kc;
+    w.max_chunks = Bc * ((Nc + kChunk - 1) / kChunk);
+    const size_t rows = (size_t)Bc * (size_t)Lc;
+    size_t o = 0;
+    w.bins = o;      o = align256(o + sizeof(BinaryRec) * (size_t)Bc);
+    w.fac = o;       o = align256(o + sizeof(FacCoeffs) * (size_t)Bc);
+    w.traj = o;      o = align256(o + sizeof(double) * kTrajStride * rows);
+    w.nsteps = o;    o = align256(o + sizeof(int) * (size_t)Bc);
+    w.status = o;    o = align256(o + sizeof(int) * (size_t)Bc);
+    w.queue = o;     o = align256(o + sizeof(unsigned long long) * 4);
+    w.row_off = o;   o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
+    w.chunk_off = o; o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
+    w.npts = o;      o = align256(o + sizeof(int) * (size_t)Bc);
+    w.tin = o;       o = align256(o + sizeof(double) * rows);
+    w.ys = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
+    w.cA = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
+    w.cB = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
+    w.cC = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
+    w.cD = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
+    w.partial = o;   o = align256(o + sizeof(double) * (size_t)w.max_chunks);
+    w.total = o;
+    return w;
+}
+
+// Typed views of the workspace.
+struct Ws {
+    BinaryRec *bins;
+    FacCoeffs *fac;
+    double *traj;
+    int *nsteps, *status;
+    unsigned long long *queue;  // [0] work queue, [1] total rows, [2] total chunks, [3] sum data^2 (double bits)
+    long long *row_off, *chunk_off;
+    int *npts;
+    double *tin, *ys, *cA, *cB, *cC, *cD, *partial;
+    WsLayout L;
+};
+
+inline Ws ws_views(void *base, const WsLayout &L)
+{
+    char *b = (char *)base;
+    Ws w;
+    w.bins = (BinaryRec *)(b + L.bins);
+    w.fac = (FacCoeffs *)(b + L.fac);
+    w.traj = (double *)(b + L.traj);
+    w.nsteps = (int *)(b + L.nsteps);
+    w.status = (int *)(b + L.status);
+    w.queue = (unsigned long long *)(b + L.queue);
+    w.row_off = (long long *)(b + L.row_off);
+    w.chunk_off = (long long *)(b + L.chunk_off);
+    w.npts = (int *)(b + L.npts);
+    w.tin = (double *)(b + L.tin);
+    w.ys = (double *)(b + L.ys);
+    w.cA = (double *)(b + L.cA);
+    w.cB = (double *)(b + L.cB);
+    w.cC = (double *)(b + L.cC);
+    w.cD = (double *)(b + L.cD);
+    w.partial = (double *)(b + L.partial);
+    w.L = L;
+    return w;
+}
+
+// Kernel launchers (defined in the k_*.cu translation units).
+struct RunArgs {
+    const double *params;  // [B][5]: m1, m2 [Msun], chi1, chi2, f0 [Hz]
+    const int *order;      // work order (longest first) or null
+    int B;
+    int K;
+    int ells[kMaxModes], mms[kMaxModes];
+    double dt;
+    const double *data;
+    int N;
+    double amp;
+    eob_options opt;
+    double *lnl;
+    int *status_out;
+};
+
+cudaError_t launch_setup(const Ws &w, const RunArgs &a, cudaStream_t s);
+cudaError_t launch_integrate(const Ws &w, const RunArgs &a, cudaStream_t s);
+cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s);
+// mode 0: lnL (a.data, a.lnl); 1: summed strain out[B][N]; 2: per-mode out[B][K][N], t clamped to each end
+cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, cudaStream_t s);
+
+}  // namespace eob

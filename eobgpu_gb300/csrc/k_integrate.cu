@@ -1,0 +1,372 @@
+// Persistent DOPR853 integrator over the EOB equations of motion.
+//
+// Replaces the reference's Python-driven loop (eob/new_Dormand_horiz.py:
+// 424-778) and its ~90 synchronous launches per step (src/DOPR853.cu:357-798,
+// src/EOB.cu:3046-3145) with one launch for the whole batch:
+//
+//  * one thread per binary (GB300 issues one FP64 warp-instruction per 64
+//    cycles per SM sub-partition whatever the active mask, so every lane must
+//    carry its own binary);
+//  * a flat per-lane state machine: each pass through the main loop evaluates
+//    exactly one right-hand side on every lane, whether that lane is in stage
+//    s of a step, in the stopping test, or starting a new pass or binary --
+//    the expensive RHS never diverges;
+//  * binaries are taken from a device work queue (atomicAdd) in a caller
+//    given order (longest first), so ragged step counts (13 .. 8676 steps)
+//    refill lanes instead of idling them;
+//  * the stopping test's RHS at the accepted state is reused as the next
+//    step's first stage (the reference evaluates the same function twice);
+//  * both passes of run_trajectory (eob/seobnrv4phm.py:2072-2136) run in the
+//    same thread: adaptive pass, step back 10 M, fixed 0.05 M pass;
+//  * the stopping rule is StoppingCriterion (eob/seobnrv4phm.py:82-150) read
+//    for one binary; its omega history restarts at zero at every pass.
+//
+// All loops are bounded: a pass ends after max_tries step attempts, on a
+// non-finite error estimate or step, or at the row capacity.
+#include "eob_device.cuh"
+
+namespace eob {
+namespace dp {
+// Tableau of Hairer's DOP853 as used by the reference (src/DOPR853.cu:10-192).
+// For stage s (2..12) the weights a[s][*] on the stored slopes, listed in the
+// reference's accumulation order; slot numbering k1..k10, stage 11 writes k2
+// and stage 12 writes k3 (src/DOPR853.cu:498, 516).
+struct Term {
+    signed char slot;
+    double a;
+};
+__constant__ Term kStage[13][9] = {
+    {}, {},
+    {{1, 5.26001519587677318785587544488e-2}},
+    {{1, 1.97250569845378994544595329183e-2}, {2, 5.91751709536136983633785987549e-2}},
+    {{1, 2.95875854768068491816892993775e-2}, {3, 8.87627564304205475450678981324e-2}},
+    {{1, 2.41365134159266685502369798665e-1}, {3, -8.84549479328286085344864962717e-1},
+     {4, 9.24834003261792003115737966543e-1}},
+    {{1, 3.7037037037037037037037037037e-2}, {4, 1.70828608729473871279604482173e-1},
+     {5, 1.25467687566822425016691814123e-1}},
+    {{1, 3.7109375e-2}, {4, 1.70252211019544039314978060272e-1}, {5, 6.02165389804559606850219397283e-2},
+     {6, -1.7578125e-2}},
+    {{1, 3.70920001185047927108779319836e-2}, {4, 1.70383925712239993810214054705e-1},
+     {5, 1.07262030446373284651809199168e-1}, {6, -1.53194377486244017527936158236e-2},
+     {7, 8.27378916381402288758473766002e-3}},
+    {{1, 6.24110958716075717114429577812e-1}, {4, -3.36089262944694129406857109825e0},
+     {5, -8.68219346841726006818189891453e-1}, {6, 2.75920996994467083049415600797e1},
+     {7, 2.01540675504778934086186788979e1}, {8, -4.34898841810699588477366255144e1}},
+    {{1, 4.77662536438264365890433908527e-1}, {4, -2.48811461997166764192642586468e0},
+     {5, -5.90290826836842996371446475743e-1}, {6, 2.12300514481811942347288949897e1},
+     {7, 1.52792336328824235832596922938e1}, {8, -3.32882109689848629194453265587e1},
+     {9, -2.03312017085086261358222928593e-2}},
+    {{1, -9.3714243008598732571704021658e-1}, {4, 5.18637242884406370830023853209e0},
+     {5, 1.09143734899672957818500254654e0}, {6, -8.14978701074692612513997267357e0},
+     {7, -1.85200656599969598641566180701e1}, {8, 2.27394870993505042818970056734e1},
+     {9, 2.49360555267965238987089396762e0}, {10, -3.0467644718982195003823669022e0}},
+    {{1, 2.27331014751653820792359768449e0}, {4, -1.05344954667372501984066689879e1},
+     {5, -2.00087205822486249909675718444e0}, {6, -1.79589318631187989172765950534e1},
+     {7, 2.79488845294199600508499808837e1}, {8, -2.85899827713502369474065508674e0},
+     {9, -8.87285693353062954433549289258e0}, {10, 1.23605671757943030647266201528e1},
+     {2, 6.43392746015763530355970484046e-1}},
+};
+__constant__ signed char kNTerms[13] = {0, 0, 1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9};
+__constant__ signed char kOutSlot[13] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 2, 3};
+
+constexpr double b1 = 5.42937341165687622380535766363e-2, b6 = 4.45031289275240888144113950566e0,
+                 b7 = 1.89151789931450038304281599044e0, b8 = -5.8012039600105847814672114227e0,
+                 b9 = 3.1116436695781989440891606237e-1, b10 = -1.52160949662516078556178806805e-1,
+                 b11 = 2.01365400804030348374776537501e-1, b12 = 4.47106157277725905176885569043e-2;
+constexpr double bhh1 = 0.244094488188976377952755905512e+00, bhh2 = 0.733846688281611857341361741547e+00,
+                 bhh3 = 0.220588235294117647058823529412e-01;
+constexpr double er1 = 0.1312004499419488073250102996e-01, er6 = -0.1225156446376204440720569753e+01,
+                 er7 = -0.4957589496572501915214079952e+00, er8 = 0.1664377182454986536961530415e+01,
+                 er9 = -0.3503288487499736816886487290e+00, er10 = 0.3341791187130174790297318841e+00,
+                 er11 = 0.8192320648511571246570742613e-01, er12 = -0.2235530786388629525884427845e-01;
+constexpr double safe = 0.9, minscale = 1.0 / 3.0, maxscale = 6.0;
+}  // namespace dp
+
+// err^(-1/8) without pow(): three square roots and a division
+__device__ __forceinline__ double inv_eighth_root(double x) { return 1.0 / sqrt(sqrt(sqrt(x))); }
+
+__device__ __forceinline__ double pow4(double x)
+{
+    const double x2 = x * x;
+    return x2 * x2;
+}
+
+// Lane state
+enum Phase : int { kIdle = 0, kStartPass = 1, kStage = 2, kStopTest = 3 };
+
+struct IntArgs {
+    const BinaryRec *bins;
+    const int *order;
+    int B;
+    double *traj;
+    int cap;
+    int *nsteps;
+    int *status;
+    unsigned long long *queue;
+    double rtol, atol, h_init, fine_step, step_back, tmax;
+    long long max_tries;
+};
+
+__global__ void __launch_bounds__(256) k_integrate(IntArgs a)
+{
+    // per-lane DOPR853 state
+    double k[11][4];  // slopes k1..k10 (slot 0 unused)
+    double y[4], ynew[4], arg[4];
+    double x = 0.0, h = 0.0, hfix = 0.0, errOld = 1e-4;
+    double om_hist[4] = {0.0, 0.0, 0.0, 0.0};  // omega of rows (step-4 .. step-1) % 4
+    int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
+    bool prevReject = false, fix = false;
+    long long tries = 0;
+    const BinaryRec *rec = nullptr;
+    double *tr = nullptr;
+    bool queue_empty = false;
+
+    for (;;) {
+        // ------------------------------------------------ bookkeeping
+        if (phase == kIdle && !queue_empty) {
+            const unsigned long long slot = atomicAdd(&a.queue[0], 1ull);
+            if (slot >= (unsigned long long)a.B) {
+                queue_empty = true;
+            } else {
+                b = a.order ? a.order[slot] : (int)slot;
+                rec = &a.bins[b];
+                tr = a.traj + (size_t)b * (size_t)a.cap * kTrajStride;
+                st = 0;
+                pass = 1;
+                step = 0;
+                x = 0.0;
+                for (int q = 0; q < 4; ++q) y[q] = rec->y0[q];
+                tr[0] = 0.0;
+                for (int q = 0; q < 4; ++q) tr[1 + q] = y[q];
+                h = a.h_init;
+                hfix = a.h_init;
+                fix = false;
+                phase = kStartPass;
+            }
+        }
+        const bool active = (phase != kIdle);
+        // all lanes of the warp idle and the queue exhausted: done
+        if (__all_sync(0xffffffffu, !active)) break;
+
+        // ------------------------------------------------ RHS argument
+        int out_slot = 1;
+        if (phase == kStage) {
+            const int nt = dp::kNTerms[stage];
+            for (int q = 0; q < 4; ++q) {
+                double ak = 0.0;
+                for (int t = 0; t < nt; ++t) ak += dp::kStage[stage][t].a * k[dp::kStage[stage][t].slot][q];
+                arg[q] = y[q] + h * ak;
+            }
+            out_slot = dp::kOutSlot[stage];
+        } else if (phase == kStopTest) {
+            for (int q = 0; q < 4; ++q) arg[q] = y[q];
+        } else if (phase == kStartPass) {
+            for (int q = 0; q < 4; ++q) arg[q] = y[q];
+        } else {
+            // idle lane: evaluate a harmless state of binary 0 (result unused)
+            rec = &a.bins[0];
+            for (int q = 0; q < 4; ++q) arg[q] = rec->y0[q];
+        }
+
+        // ------------------------------------------------ the one RHS per loop
+        double kk[4];
+        eob_rhs(rec->ham, rec->flux, arg, kk);
+        if (!active) continue;
+
+        // ------------------------------------------------ advance the lane
+        if (phase == kStartPass) {
+            for (int q = 0; q < 4; ++q) k[1][q] = kk[q];
+            errOld = 1e-4;
+            prevReject = false;
+            tries = 0;
+            first_row = step + 1;
+            for (int q = 0; q < 4; ++q) om_hist[q] = 0.0;
+            stage = 2;
+            phase = kStage;
+            continue;
+        }
+        if (phase == kStage) {
+            for (int q = 0; q < 4; ++q) k[out_slot][q] = kk[q];
+            if (stage < 12) {
+                ++stage;
+                continue;
+            }
+            // error estimate (src/DOPR853.cu:537-618)
+            double e1 = 0.0, e2 = 0.0;
+            for (int q = 0; q < 4; ++q) {
+                const double t = dp::b1 * k[1][q] + dp::b6 * k[6][q] + dp::b7 * k[7][q] + dp::b8 * k[8][q] +
+                                 dp::b9 * k[9][q] + dp::b10 * k[10][q] + dp::b11 * k[2][q] + dp::b12 * k[3][q];
+                ynew[q] = y[q] + h * t;
+                const double mx = (y[q] > ynew[q]) ? y[q] : ynew[q];
+                const double sk = 1.0 / (a.atol + a.rtol * mx);
+                e2 += pow4((t - dp::bhh1 * k[1][q] - dp::bhh2 * k[9][q] - dp::bhh3 * k[3][q]) * sk);
+                e1 += pow4((dp::er1 * k[1][q] + dp::er6 * k[6][q] + dp::er7 * k[7][q] + dp::er8 * k[8][q] +
+                            dp::er9 * k[9][q] + dp::er10 * k[10][q] + dp::er11 * k[2][q] + dp::er12 * k[3][q]) * sk);
+            }
+            double denom = e1 + 0.01 * e2;
+            denom = (denom < 0.0) ? 1.0 : denom;
+            const double err = fabs(h) * e1 * sqrt(1.0 / (4.0 * denom));
+            const double hOld = h;
+            // controller (src/DOPR853.cu:674-762), beta = 0
+            bool ok;
+            if (err <= 1.0) {
+                double scale;
+                if (err == 0.0) {
+                    scale = dp::maxscale;
+                } else {
+                    scale = dp::safe * inv_eighth_root(err);
+                    if (scale > dp::maxscale) scale = dp::maxscale;
+                    else if (scale < dp::minscale) scale = dp::minscale;
+                }
+                if (prevReject && scale > 1.0) scale = 1.0;
+                h = h * scale;
+                double eo = err;
+                if (eo < 1e-4) eo = 1e-4; else if (eo > 1e300) eo = 1e300;
+                errOld = eo;
+                prevReject = false;
+                ok = true;
+            } else {
+                prevReject = true;
+                double t = dp::safe * inv_eighth_root(err);
+                if (t < dp::minscale) t = dp::minscale; else if (t > 1e300) t = 1e300;
+                h = h * t;
+                ok = false;
+            }
+            (void)errOld;
+            if (fix && !ok) hfix /= 2.0;
+            if (fix) h = hfix;
+            ++tries;
+            const bool bad = !(err == err) || !(h == h) || h == 0.0;
+            if (ok) {
+                for (int q = 0; q < 4; ++q) y[q] = ynew[q];
+                x = x + hOld;
+                ++step;
+                double *row = tr + (size_t)step * kTrajStride;
+                row[0] = x;
+                for (int q = 0; q < 4; ++q) row[1 + q] = y[q];
+                phase = kStopTest;  // next RHS: f(y_new) for the stopping rule and the next k1
+                if (bad) st |= EOB_ST_NAN;
+            } else {
+                // first attempt of the pass rejected: the reference's stop flags
+                // start true, so the pass ends here (new_Dormand_horiz.py:623-761)
+                bool end = (step == first_row - 1);
+                if (end) st |= EOB_ST_STOP_REJECT;
+                if (bad) { st |= EOB_ST_NAN; end = true; }
+                if (tries >= a.max_tries) { st |= EOB_ST_TRIES; end = true; }
+                if (!end) {
+                    stage = 2;  // retry with the new h; k1 unchanged
+                    continue;
+                }
+                phase = -1;  // fall through to end-of-pass handling
+            }
+            if (phase == kStopTest && !bad) continue;
+            if (phase == kStopTest && bad) phase = -1;
+        }
+        bool end_pass = false;
+        if (phase == kStopTest) {
+            // stopping rule on the accepted state (kk = f(y))
+            for (int q = 0; q < 4; ++q) k[1][q] = kk[q];
+            const double r = y[0], drdt = kk[0], omega = kk[1], dprdt = kk[2];
+            int code = 0;
+            if (r < 1.0) code = 2;
+            else if (r < 6.0 && drdt > 0.0) code = 3;
+            else if (r < 6.0 && dprdt > 0.0) code = 4;
+            else if (step > 5) {
+                // history rows written in this pass, zero before (omega array restarts per pass)
+                double o[5];
+                for (int j = 1; j <= 4; ++j) o[j] = (step - j >= first_row) ? om_hist[(step - j) & 3] : 0.0;
+                const bool c2 = omega < o[1];
+                const bool c3 = (o[3] - o[4] < 0.0) && (o[2] - o[3] < 0.0) && (o[1] - o[2] < 0.0);
+                if (r < 6.0 && c2 && c3) code = 5;
+            }
+            om_hist[step & 3] = omega;
+            end_pass = (code != 0) || (x >= a.tmax) || (step >= a.cap - 1) || (tries >= a.max_tries);
+            if (step >= a.cap - 1) st |= EOB_ST_MAXSTEP;
+            if (tries >= a.max_tries && code == 0) st |= EOB_ST_TRIES;
+            if (!end_pass) {
+                stage = 2;
+                phase = kStage;
+                continue;
+            }
+        } else {
+            end_pass = true;  // rejected first attempt, non-finite state or attempt limit
+        }
+        // ------------------------------------------------ end of a pass
+        if (pass == 1 && end_pass) {
+            // step back (eob/seobnrv4phm.py:2096-2114): t_stop is the time of
+            // the second-to-last stored row; restart from the row before the one
+            // closest to t_stop - step_back
+            const int S1 = step;
+            if (S1 < 2 || (st & (EOB_ST_NAN | EOB_ST_TRIES))) {
+                st |= EOB_ST_SHORT;
+                a.nsteps[b] = S1 + 1;
+                a.status[b] |= st;
+                phase = kIdle;
+                continue;
+            }
+            const double t_stop = tr[(size_t)(S1 - 1) * kTrajStride];
+            const double t_des = t_stop - a.step_back;
+            int idx = 0;
+            double best = fabs(tr[0] - t_des);
+            for (int i = 1; i <= S1; ++i) {
+                const double d = fabs(tr[(size_t)i * kTrajStride] - t_des);
+                if (d < best) { best = d; idx = i; }
+            }
+            if (idx < 1) { idx = 1; st |= EOB_ST_SHORT; }
+            step = idx - 1;
+            const double *row = tr + (size_t)step * kTrajStride;
+            x = row[0];
+            for (int q = 0; q < 4; ++q) y[q] = row[1 + q];
+            pass = 2;
+            h = a.fine_step;
+            hfix = a.fine_step;
+            fix = true;
+            st &= ~EOB_ST_STOP_REJECT;
+            phase = kStartPass;
+            continue;
+        }
+        // pass 2 finished: binary done
+        a.nsteps[b] = step + 1;
+        a.status[b] |= st;
+        phase = kIdle;
+    }
+}
+
+cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
+{
+    IntArgs a;
+    a.bins = w.bins;
+    a.order = ra.order;
+    a.B = ra.B;
+    a.traj = w.traj;
+    a.cap = w.L.Lc;
+    a.nsteps = w.nsteps;
+    a.status = w.status;
+    a.queue = w.queue;
+    a.rtol = ra.opt.rtol;
+    a.atol = ra.opt.atol;
+    a.h_init = ra.opt.h_init;
+    a.fine_step = ra.opt.fine_step;
+    a.step_back = ra.opt.step_back;
+    a.tmax = 1e7 * 1e6;
+    a.max_tries = ra.opt.max_tries > 0 ? ra.opt.max_tries : 2LL * w.L.Lc + 100;
+    const int bs = (ra.opt.block > 0 && ra.opt.block <= 256) ? ra.opt.block : 128;
+    int grid = ra.opt.grid;
+    if (grid <= 0) {
+        // enough lanes for every binary, at most one wave of resident blocks
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate, bs, 0);
+        if (per_sm < 1) per_sm = 1;
+        const int need = (ra.B + bs - 1) / bs;
+        grid = need < nsm * per_sm ? need : nsm * per_sm;
+        if (grid < 1) grid = 1;
+    }
+    cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_integrate<<<grid, bs, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace eob

@@ -1,0 +1,372 @@
+// After the integrator: packing, multipoles on the trajectory, batched
+// not-a-knot splines, and the fused synthesis + likelihood pass.
+//
+//  k_scan_*    one block: per-binary row counts and waveform sample counts,
+//              exclusive scans (packed ragged layout), sum of data^2.
+//  k_modes     one thread per packed trajectory row: h_lm e^{i m phi} for the
+//              requested modes (get_hlms, eob/seobnrv4phm.py:2138-2221, and
+//              the de-rotation of compute_full_waveform, :2331).
+//  k_spline    one thread per (binary, series): not-a-knot cubic spline with
+//              the reference's tridiagonal set-up and Thomas sweep
+//              (src/interpolate.cu:10-267).
+//  k_synth     one block per 1024-sample chunk of one binary: spline
+//              evaluation on the uniform grid (eob/seobnrv4phm.py:274-386,
+//              2310-2372), mode sum (BBHWaveformTD, :715-721) and the
+//              white-noise residual, reduced to one partial per chunk; in
+//              likelihood mode the strain is never written to memory.
+//  k_finalize  per binary, partials summed in a fixed order (deterministic).
+#include "eob_device.cuh"
+
+namespace eob {
+
+constexpr int kScanThreads = 1024;
+
+__device__ __forceinline__ double t_in_of(double t_M, double Mt)
+{
+    // reference: t[s] = t_M * mt * MTSUN_SI, then t / (M * MTSUN_SI)
+    return (t_M * Mt * kMTSUN_SI) / (Mt * kMTSUN_SI);
+}
+
+// number of uniform samples of binary b: int((t_end - t_0) / dT) + 1
+__device__ int binary_npts(const double *tr, int L, double Mt, double dt)
+{
+    const double t0 = t_in_of(tr[0], Mt);
+    const double t1 = t_in_of(tr[(size_t)(L - 1) * kTrajStride], Mt);
+    const double dT = dt / (Mt * kMTSUN_SI);
+    return (int)((t1 - t0) / dT) + 1;
+}
+
+// block-wide exclusive scan helper: returns the exclusive prefix of v over the block
+template <int NT>
+__device__ long long block_exclusive_scan(long long v, long long *sm, long long *total)
+{
+    const int tid = threadIdx.x;
+    sm[tid] = v;
+    __syncthreads();
+    for (int off = 1; off < NT; off <<= 1) {
+        const long long add = (tid >= off) ? sm[tid - off] : 0;
+        __syncthreads();
+        sm[tid] += add;
+        __syncthreads();
+    }
+    const long long incl = sm[tid];
+    if (total) *total = sm[NT - 1];
+    __syncthreads();
+    return incl - v;
+}
+
+// rows and uniform-grid sample counts per binary; packed row offsets
+__global__ void __launch_bounds__(kScanThreads) k_scan_rows(Ws w, int B, double dt)
+{
+    __shared__ long long sm[kScanThreads];
+    const int tid = threadIdx.x;
+    const int per = (B + kScanThreads - 1) / kScanThreads;
+    const int b0 = tid * per;
+    const int b1 = min(B, b0 + per);
+    long long rows = 0;
+    for (int b = b0; b < b1; ++b) {
+        const int L = w.nsteps[b];
+        int st = w.status[b];
+        int np = 0;
+        if (L >= 3 && !(st & (EOB_ST_NAN | EOB_ST_TRIES | EOB_ST_SHORT))) {
+            np = binary_npts(w.traj + (size_t)b * w.L.Lc * kTrajStride, L, w.bins[b].Mt, dt);
+            if (np < 1) np = 0;
+        } else {
+            st |= EOB_ST_SHORT;
+            w.status[b] = st;
+        }
+        w.npts[b] = np;
+        rows += (np > 0) ? L : 0;
+    }
+    long long total;
+    long long ro = block_exclusive_scan<kScanThreads>(rows, sm, &total);
+    for (int b = b0; b < b1; ++b) {
+        w.row_off[b] = ro;
+        ro += (w.npts[b] > 0) ? w.nsteps[b] : 0;
+    }
+    if (tid == 0) {
+        w.row_off[B] = total;
+        w.queue[1] = (unsigned long long)total;
+    }
+}
+
+// synthesis work items: chunks of kChunk samples of min(npts, N) samples per
+// binary (all N samples when cover_all); sum of data^2
+__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Ws w, int B, int N, int cover_all, const double *data)
+{
+    __shared__ long long sm[kScanThreads];
+    __shared__ double s_sq[kScanThreads];
+    const int tid = threadIdx.x;
+    const int per = (B + kScanThreads - 1) / kScanThreads;
+    const int b0 = tid * per;
+    const int b1 = min(B, b0 + per);
+    long long chunks = 0;
+    for (int b = b0; b < b1; ++b) {
+        const int np = w.npts[b];
+        const int nuse = (np <= 0) ? 0 : (cover_all ? N : (np < N ? np : N));
+        chunks += (nuse + kChunk - 1) / kChunk;
+    }
+    double sq = 0.0;
+    if (data)
+        for (int k = tid; k < N; k += kScanThreads) sq += data[k] * data[k];
+    s_sq[tid] = sq;
+    long long total;
+    long long co = block_exclusive_scan<kScanThreads>(chunks, sm, &total);
+    for (int b = b0; b < b1; ++b) {
+        w.chunk_off[b] = co;
+        const int np = w.npts[b];
+        const int nuse = (np <= 0) ? 0 : (cover_all ? N : (np < N ? np : N));
+        co += (nuse + kChunk - 1) / kChunk;
+    }
+    for (int off = kScanThreads / 2; off > 0; off >>= 1) {
+        if (tid < off) s_sq[tid] += s_sq[tid + off];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        w.chunk_off[B] = total;
+        w.queue[2] = (unsigned long long)total;
+        w.queue[3] = (unsigned long long)__double_as_longlong(s_sq[0]);
+    }
+}
+
+// index b with off[b] <= v < off[b+1]
+__device__ __forceinline__ int find_segment(const long long *off, int B, long long v)
+{
+    int lo = 0, hi = B;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+struct ModeArgs {
+    int K;
+    int ells[kMaxModes], mms[kMaxModes];
+};
+
+__global__ void __launch_bounds__(128) k_modes(Ws w, int B, ModeArgs ma)
+{
+    const long long R = (long long)w.queue[1];
+    const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < R; r += (long long)gridDim.x * blockDim.x) {
+        const int b = find_segment(w.row_off, B, r);
+        const int i = (int)(r - w.row_off[b]);
+        const BinaryRec &rec = w.bins[b];
+        const double *row = w.traj + ((size_t)b * w.L.Lc + i) * kTrajStride;
+        const double rr = row[1], phi = row[2], pr = row[3], pphi = row[4];
+        w.tin[r] = t_in_of(row[0], rec.Mt);
+        w.ys[r] = phi;
+        HamEval e;
+        ham_eval(rec.ham, rr, pr, pphi, &e);
+        const double v = cbrt(e.dHdL);
+        const double vphi_in = 1.0 / (e.omega_c * e.omega_c * rr * rr * rr);
+        for (int j = 0; j < ma.K; ++j) {
+            const int l = ma.ells[j], m = ma.mms[j];
+            const int li = lm_index(l, m);
+            const cdbl hl = mode_eval(w.fac[b], l, m, rec.pre_re[li], rec.pre_im[li], rec.nu, rr, phi, pphi, v,
+                                      e.Hreal, vphi_in, 0.0, true);
+            w.ys[(size_t)(1 + 2 * j) * Rc + r] = hl.re;
+            w.ys[(size_t)(2 + 2 * j) * Rc + r] = hl.im;
+        }
+    }
+}
+
+// Not-a-knot spline of n knots (src/interpolate.cu:10-267): Bv rhs -> slopes;
+// ud/dg/ld end up holding c1/c2/c3 on rows 0..n-2.
+__device__ void spline_one(const double *x, const double *y, int n, double *Bv, double *ud, double *dg, double *ld)
+{
+    for (int i = 0; i < n; ++i) {
+        int i0, i1, i2;
+        if (i == n - 1) { i0 = n - 3; i1 = n - 2; i2 = n - 1; }
+        else if (i == 0) { i0 = 0; i1 = 1; i2 = 2; }
+        else { i0 = i - 1; i1 = i; i2 = i + 1; }
+        const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
+        const double dx1 = x1 - x0, dx2 = x2 - x1, d = x2 - x0;
+        const double y1 = y[i1];
+        const double s1 = (y1 - y[i0]) / dx1, s2 = (y[i2] - y1) / dx2;
+        if (i == n - 1) {
+            Bv[i] = (dx2 * dx2 * s1 + (2 * d + dx2) * dx1 * s2) / d;
+            dg[i] = dx1; ld[i] = d; ud[i] = 0.0;
+        } else if (i == 0) {
+            Bv[i] = ((dx1 + 2 * d) * dx2 * s1 + dx1 * dx1 * s2) / d;
+            ud[i] = d; ld[i] = 0.0; dg[i] = dx2;
+        } else {
+            Bv[i] = 3.0 * (dx2 * s1 + dx1 * s2);
+            dg[i] = 2 * (dx1 + dx2); ud[i] = dx1; ld[i] = dx2;
+        }
+    }
+    for (int i = 1; i < n; ++i) {
+        const double wgt = ld[i] / dg[i - 1];
+        dg[i] = dg[i] - wgt * ud[i - 1];
+        Bv[i] = Bv[i] - wgt * Bv[i - 1];
+    }
+    Bv[n - 1] = Bv[n - 1] / dg[n - 1];
+    for (int i = n - 2; i >= 0; --i) Bv[i] = (Bv[i] - ud[i] * Bv[i + 1]) / dg[i];
+    for (int i = 0; i < n - 1; ++i) {
+        const double dx = x[i + 1] - x[i];
+        const double slope = (y[i + 1] - y[i]) / dx;
+        const double bi = Bv[i];
+        const double t = (bi + Bv[i + 1] - 2 * slope) / dx;
+        ud[i] = bi;
+        dg[i] = (slope - bi) / dx - t;
+        ld[i] = t / dx;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_spline(Ws w, int B, int nsubs)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B * nsubs) return;
+    const int b = idx / nsubs, sub = idx % nsubs;
+    if (w.npts[b] <= 0) return;
+    const int n = w.nsteps[b];
+    const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
+    const size_t base = (size_t)w.row_off[b];
+    const size_t o = (size_t)sub * Rc + base;
+    spline_one(w.tin + base, w.ys + o, n, w.cD + o, w.cA + o, w.cB + o, w.cC + o);
+}
+
+struct SynthArgs {
+    int B, N, K;
+    int mms[kMaxModes];
+    double dt, amp;
+    const double *data;   // lnL mode
+    double *out;          // strain modes
+    int mode;             // 0: lnL, 1: summed strain (zero past the end), 2: per mode, t clamped to the end
+};
+
+// interval i with x[i] <= t < x[i+1] (searchsorted right - 1), t, x >= 0:
+// integer comparison of the IEEE bit patterns keeps the FP64 pipe free.
+__device__ __forceinline__ int knot_index(const double *x, int n, double t)
+{
+    const long long tb = __double_as_longlong(t);
+    int lo = 0, hi = n;  // first index with x > t lies in [lo, hi]
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__double_as_longlong(x[mid]) <= tb) lo = mid + 1; else hi = mid;
+    }
+    int i = lo - 1;
+    if (i < 0) i = 0;
+    if (i > n - 1) i = n - 1;
+    return i;
+}
+
+__global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
+{
+    __shared__ double s_red[256 / 32];
+    const long long C = (long long)w.queue[2];
+    const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
+    for (long long c = blockIdx.x; c < C; c += gridDim.x) {
+        const int b = find_segment(w.chunk_off, sa.B, c);
+        const int j = (int)(c - w.chunk_off[b]);
+        const int np = w.npts[b];
+        const int nuse = (sa.mode == 2) ? sa.N : (np < sa.N ? np : sa.N);
+        const int n = w.nsteps[b];
+        const size_t base = (size_t)w.row_off[b];
+        const double *x = w.tin + base;
+        const double Mts = w.bins[b].Mt * kMTSUN_SI;
+        const double dT = sa.dt / Mts;
+        const double t0 = x[0], tend = x[n - 1];
+        double acc = 0.0;
+        const int kbeg = j * kChunk;
+        const int kend = min(nuse, kbeg + kChunk);
+        for (int k = kbeg + threadIdx.x; k < kend; k += blockDim.x) {
+            double t = k * dT + t0;
+            if (t > tend) t = tend;
+            const int i = knot_index(x, n, t);
+            const double xx = t - x[i], x2 = xx * xx, x3 = x2 * xx;
+            const size_t o = base + i;
+            const double phi = w.ys[o] + w.cA[o] * xx + w.cB[o] * x2 + w.cC[o] * x3;
+            double hsum = 0.0, hsum_i = 0.0;
+            for (int q = 0; q < sa.K; ++q) {
+                const size_t orr = (size_t)(1 + 2 * q) * Rc + o, oi = (size_t)(2 + 2 * q) * Rc + o;
+                const double re = w.ys[orr] + w.cA[orr] * xx + w.cB[orr] * x2 + w.cC[orr] * x3;
+                const double im = w.ys[oi] + w.cA[oi] * xx + w.cB[oi] * x2 + w.cC[oi] * x3;
+                double sp, cp;
+                sincos(sa.mms[q] * phi, &sp, &cp);
+                // (re + i im) e^{-i m phi}
+                const double hr = re * cp + im * sp, hi = im * cp - re * sp;
+                if (sa.mode == 2) {
+                    const size_t oo = 2 * (((size_t)b * sa.K + q) * (size_t)sa.N + k);
+                    sa.out[oo] = hr;
+                    sa.out[oo + 1] = hi;
+                }
+                hsum += hr;
+                hsum_i += hi;
+            }
+            if (sa.mode == 1) {
+                sa.out[2 * ((size_t)b * sa.N + k)] = hsum;
+                sa.out[2 * ((size_t)b * sa.N + k) + 1] = hsum_i;
+            } else if (sa.mode == 0) {
+                const double hk = sa.amp * hsum;
+                acc += hk * hk - 2.0 * sa.data[k] * hk;
+            }
+        }
+        // block reduction (fixed order)
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0 && sa.mode == 0) {
+            double s = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += s_red[q];
+            w.partial[c] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_finalize(Ws w, int B, double *lnl, int *status_out)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const double dsq = __longlong_as_double((long long)w.queue[3]);
+    const int st = w.status[b];
+    double s = 0.0;
+    for (long long c = w.chunk_off[b]; c < w.chunk_off[b + 1]; ++c) s += w.partial[c];
+    const bool bad = (w.npts[b] <= 0);
+    if (lnl) lnl[b] = bad ? __longlong_as_double(0x7ff8000000000000LL) : -0.5 * (dsq + s);
+    if (status_out) status_out[b] = st;
+}
+
+cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k_scan_rows<<<1, kScanThreads, 0, s>>>(w, a.B, a.dt);
+    ModeArgs ma;
+    ma.K = a.K;
+    for (int j = 0; j < kMaxModes; ++j) { ma.ells[j] = a.ells[j]; ma.mms[j] = a.mms[j]; }
+    k_modes<<<nsm * 8, 128, 0, s>>>(w, a.B, ma);
+    const int nsubs = 1 + 2 * a.K;
+    k_spline<<<(a.B * nsubs + 127) / 128, 128, 0, s>>>(w, a.B, nsubs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, cudaStream_t s)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k_scan_chunks<<<1, kScanThreads, 0, s>>>(w, a.B, a.N, mode == 2 ? 1 : 0, mode == 0 ? a.data : nullptr);
+    if (mode == 1) {
+        cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * 2 * (size_t)a.B * a.N, s);
+        if (e != cudaSuccess) return e;
+    }
+    SynthArgs sa;
+    sa.B = a.B;
+    sa.N = a.N;
+    sa.K = a.K;
+    for (int j = 0; j < kMaxModes; ++j) sa.mms[j] = a.mms[j];
+    sa.dt = a.dt;
+    sa.amp = a.amp;
+    sa.data = a.data;
+    sa.out = out;
+    sa.mode = mode;
+    k_synth<<<nsm * 8, 256, 0, s>>>(w, sa);
+    k_finalize<<<(a.B + 127) / 128, 128, 0, s>>>(w, a.B, mode == 0 ? a.lnl : nullptr, a.status_out);
+    return cudaGetLastError();
+}
+
+}  // namespace eob

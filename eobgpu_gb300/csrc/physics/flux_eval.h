@@ -1,0 +1,212 @@
+// Radiation-reaction flux and force from per-binary tables, written for FP64
+// issue rate.
+//
+// Restates EOBSpinFactorizedFlux / EOBFluxGetSpinFactorizedWaveform /
+// RR_force (src/EOB.cu:2505-2642, 1705-1943): F = omega^2/(8 pi)
+// sum_{l<=8, 1<=m<=l} m^2 |h_lm|^2 with the flux multipoles' truncated
+// rho_lm.  Only |h_lm|^2 is needed, so every factor is squared in place:
+//   |T_lm|^2 = (4 pi k)/(1 - exp(-4 pi k)) / (l!)^2 * prod_{j<=l} (4 k^2 + j^2),
+//   k = m H_real omega,
+// the same closed form the reference uses for its flux (src/EOB.cu:1740-1748).
+// Shared pieces are computed once per call: one exp(-4 pi H omega) raised to
+// the m-th power, one log(v) for every eulerlog_m, the products over j
+// accumulated across l for each m, powers of vPhi^2 by multiplication.
+#pragma once
+#include "fac_coeffs.h"
+#include "ham_eval.h"
+
+namespace eob {
+
+struct FluxTable {
+    double rho[kNumLM][11];   // flux rho_lm: 1 + sum_{k=1..10} (rho[k] + rhol[k] eulerlog_m) v^k
+    double rhol[kNumLM][11];
+    double f1[kNumLM], f3[kNumLM];  // f_lm = f1 v + f3 v^3
+    double nabs2[kNumLM];     // |Newtonian prefix|^2 Y_{l-eps}^m(pi/2)^2
+    double h22calib;          // h22 calibration: rho_22 += h22calib v^12
+    double eta;               // clamped symmetric mass ratio used by S_lm
+    double equal_mass;        // 1.0 when eta == 0.25 (odd m use f_lm alone)
+    double elog[kLMax + 1];   // gamma + log(2 m), m = 1..8: eulerlog_m(v) = elog[m] + log v
+
+    EOB_HD double c_rho(int i, int k) const { return rho[i][k]; }
+    EOB_HD double c_rhol(int i, int k) const { return rhol[i][k]; }
+    EOB_HD double c_f1(int i) const { return f1[i]; }
+    EOB_HD double c_f3(int i) const { return f3[i]; }
+    EOB_HD double c_nabs2(int i, int, int) const { return nabs2[i]; }
+    EOB_HD double c_elog(int m) const { return elog[m]; }
+    EOB_HD double c_eta() const { return eta; }
+    EOB_HD double c_equal() const { return equal_mass; }
+    EOB_HD double c_h22() const { return h22calib; }
+};
+
+// The same flux inputs read straight from a FacCoeffs table and
+// reference-layout prefixes (additionalArgs rows 10.., stride n); used by the
+// reference-shaped entry points, which receive coefficients and prefixes
+// separately (src/EOB.cu:2505-2561).
+struct FacFluxView {
+    const FacCoeffs *fc;
+    const double *add;  // additionalArgs + system index
+    int n;              // row stride of additionalArgs
+    double eta, equal_mass, h22;
+    EOB_HD double c_rho(int i, int k) const { return fc->rho[i][k]; }
+    EOB_HD double c_rhol(int i, int k) const { return fc->rhol[i][k]; }
+    EOB_HD double c_f1(int i) const { return fc->fre[i][1]; }
+    EOB_HD double c_f3(int i) const { return fc->fre[i][3]; }
+    EOB_HD double c_nabs2(int i, int l, int m) const
+    {
+        const double re = add[(size_t)(10 + 2 * i) * n], im = add[(size_t)(11 + 2 * i) * n];
+        const double y = ylm_equator(l - (l + m) % 2, m);
+        return (re * re + im * im) * y * y;
+    }
+    EOB_HD double c_elog(int m) const { return kEulerGamma + log(2.0 * m); }
+    EOB_HD double c_eta() const { return eta; }
+    EOB_HD double c_equal() const { return equal_mass; }
+    EOB_HD double c_h22() const { return h22; }
+};
+
+EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *prefix_re, const double *prefix_im,
+                             double h22calib, double nu)
+{
+    for (int l = 2; l <= kLMax; ++l)
+        for (int m = 1; m <= l; ++m) {
+            const int i = lm_index(l, m);
+            const int kmax = flux_rho_maxdeg(l, m);
+            for (int k = 0; k <= 10; ++k) {
+                t->rho[i][k] = (k >= 1 && k <= kmax) ? fc.rho[i][k] : 0.0;
+                t->rhol[i][k] = (k >= 1 && flux_keeps_rhol(l, m, k)) ? fc.rhol[i][k] : 0.0;
+            }
+            t->f1[i] = flux_keeps_f(l, m, 1) ? fc.fre[i][1] : 0.0;
+            t->f3[i] = flux_keeps_f(l, m, 3) ? fc.fre[i][3] : 0.0;
+            const int eps = (l + m) % 2;
+            const double y = ylm_equator(l - eps, m);
+            t->nabs2[i] = (prefix_re[i] * prefix_re[i] + prefix_im[i] * prefix_im[i]) * y * y;
+        }
+    t->h22calib = h22calib;
+    double eta = nu;
+    if (eta > 0.25 && eta < 0.25 + 1e-4) eta = 0.25;
+    t->eta = eta;
+    t->equal_mass = (eta == 0.25) ? 1.0 : 0.0;
+    t->elog[0] = 0.0;
+    for (int m = 1; m <= kLMax; ++m) t->elog[m] = kEulerGamma + log(2.0 * m);
+}
+
+// (l)!^2 for l = 0..8
+EOB_HD constexpr double fact2_sq(int l)
+{
+    return l <= 1 ? 1.0 : (double)l * (double)l * fact2_sq(l - 1);
+}
+
+struct FluxShared {
+    double v, lv, vphi2, Se, Sodd, x, omega;
+};
+
+// contribution m^2 |h_lm|^2 / (omega^2) of one (l, m); P = prod_{j<=l} (4k^2 + j^2)
+template <int l, int m, class Tab>
+EOB_HD double flux_term(const Tab &t, const FluxShared &s, double Tpre, double P, const double *vp2)
+{
+    constexpr int i = (l - 2) * (l + 1) / 2 + (m - 1);
+    constexpr int eps = (l + m) % 2;
+    constexpr int kmax = (l == 2) ? 10 : (l == 3) ? 8 : (l == 4) ? 6 : (l == 5) ? ((m == 5) ? 6 : (m == 3 || m == 1) ? 5 : 4)
+                                   : (l == 6) ? ((m % 2 == 0) ? 4 : 3) : (l == 7) ? ((m % 2 == 1) ? 3 : 2) : 2;
+    constexpr bool has_log = (l <= 4);
+    // eulerlog_m = gamma + log(2 m v)
+    const double elm = t.c_elog(m) + s.lv;
+    double rho = 0.0;
+#pragma unroll
+    for (int k = kmax; k >= 1; --k) {
+        double ck = t.c_rho(i, k);
+        if (has_log && (k == 6 || k == 7 || k == 8 || k == 10)) ck = fma(t.c_rhol(i, k), elm, ck);
+        rho = (rho + ck) * s.v;
+    }
+    rho += 1.0;
+    if (l == 2 && m == 2) {
+        const double v4 = (s.v * s.v) * (s.v * s.v);
+        rho = fma(t.c_h22(), v4 * v4 * v4, rho);
+    }
+    double rpl = rho;
+#pragma unroll
+    for (int q = 1; q < l; ++q) rpl *= rho;
+    const bool has_f = (l == 2 && m == 1) || (l == 3 && (m == 3 || m == 1)) || (l == 4 && (m == 3 || m == 1));
+    if (has_f) {
+        const double v2 = s.v * s.v;
+        const double aux = s.v * fma(t.c_f3(i), v2, t.c_f1(i));
+        rpl = (m % 2 == 1 && t.c_equal() != 0.0) ? aux : rpl + aux;
+    } else if (m % 2 == 1) {
+        rpl = (t.c_equal() != 0.0) ? 0.0 : rpl;
+    }
+    const double S = eps ? s.Sodd : s.Se;
+    const double hn2 = t.c_nabs2(i, l, m) * vp2[l + eps];
+    const double T2 = Tpre * P * (1.0 / fact2_sq(l));
+    return (double)(m * m) * T2 * (S * S) * (rpl * rpl) * hn2;
+}
+
+// Accumulate all l for one m (products over j carried across l).
+template <int m, int l, class Tab>
+EOB_HD double flux_m_l(const Tab &t, const FluxShared &s, double Tpre, double P, double k2x4, const double *vp2)
+{
+    P *= k2x4 + (double)(l * l);
+    double here = 0.0;
+    if constexpr (l >= (m > 2 ? m : 2)) here = flux_term<l, m, Tab>(t, s, Tpre, P, vp2);
+    if constexpr (l < kLMax) return here + flux_m_l<m, l + 1, Tab>(t, s, Tpre, P, k2x4, vp2);
+    else return here;
+}
+
+template <int m, class Tab>
+EOB_HD double flux_m(const Tab &t, const FluxShared &s, double Em, double hw, const double *vp2)
+{
+    const double mx = m * s.x;
+    const double Tpre = mx / (1.0 - Em);  // (4 pi k)/(1 - exp(-4 pi k)), k = m H omega
+    const double km = m * hw;
+    return flux_m_l<m, 1, Tab>(t, s, Tpre, 1.0, 4.0 * km * km, vp2);
+}
+
+// Radiation-reaction flux (before the division by nu of RR_force).
+// omega: orbital frequency in the flux (dH/dpphi at the state); Hreal = nu H;
+// omega_c: circular frequency (dH/dpphi at p_r = 0).
+template <class Tab>
+EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, double Hreal, double omega_c)
+{
+    FluxShared s;
+    s.omega = omega;
+    s.v = cbrt(omega);
+    s.lv = log(s.v);
+    const double vphi_in = 1.0 / (omega_c * omega_c * r * r * r);
+    const double vphi = r * cbrt(vphi_in) * omega;
+    s.vphi2 = vphi * vphi;
+    s.Se = (Hreal * Hreal - 1.0) / (2.0 * t.c_eta()) + 1.0;
+    s.Sodd = s.v * pphi;
+    s.x = 4.0 * kPi * Hreal * omega;
+    double vp2[10];
+    vp2[0] = 1.0;
+#pragma unroll
+    for (int q = 1; q < 10; ++q) vp2[q] = vp2[q - 1] * s.vphi2;
+    const double E1 = exp(-s.x);
+    const double hw = Hreal * omega;
+    const double E2 = E1 * E1, E3 = E2 * E1, E4 = E2 * E2, E5 = E4 * E1, E6 = E3 * E3, E7 = E6 * E1, E8 = E4 * E4;
+    double sum = flux_m<1, Tab>(t, s, E1, hw, vp2);
+    sum += flux_m<2, Tab>(t, s, E2, hw, vp2);
+    sum += flux_m<3, Tab>(t, s, E3, hw, vp2);
+    sum += flux_m<4, Tab>(t, s, E4, hw, vp2);
+    sum += flux_m<5, Tab>(t, s, E5, hw, vp2);
+    sum += flux_m<6, Tab>(t, s, E6, hw, vp2);
+    sum += flux_m<7, Tab>(t, s, E7, hw, vp2);
+    sum += flux_m<8, Tab>(t, s, E8, hw, vp2);
+    return sum * omega * omega / (8.0 * kPi);
+}
+
+// ODE right-hand side (src/EOB.cu:3046-3145): k = (dH/dpr, dH/dpphi,
+// -dH/dr + F_r, F_phi), F = flux/nu, F_r = -pr/pphi F/omega, F_phi = -F/omega.
+template <class Tab>
+EOB_HD void eob_rhs(const HamCoeffs &h, const Tab &t, const double y[4], double k[4])
+{
+    HamEval e;
+    ham_eval(h, y[0], y[2], y[3], &e);
+    const double omega = e.dHdL;
+    const double flux = flux_eval(t, y[0], y[3], omega, e.Hreal, e.omega_c) / h.nu;
+    const double fo = flux / omega;
+    k[0] = e.dHdpr;
+    k[1] = omega;
+    k[2] = -e.dHdr - y[2] / y[3] * fo;
+    k[3] = -fo;
+}
+
+}  // namespace eob

@@ -1,0 +1,154 @@
+"""Host side of the fused EOB waveform + likelihood path.
+
+`WaveformLikelihood` owns one device workspace (a torch uint8 tensor sized by
+eob_workspace_bytes) and runs, on one CUDA stream and with no host
+synchronisation, the five stages of the native path:
+
+  setup (tables + initial conditions) -> persistent DOPR853 integrator ->
+  multipoles on the trajectory -> not-a-knot splines -> synthesis + lnL.
+
+Inputs and outputs are torch CUDA tensors; the C ABI sees raw pointers.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+
+MTSUN_SI = 4.925491025543576e-06
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream_handle(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def chirp_duration_M(params: torch.Tensor) -> torch.Tensor:
+    """Newtonian time to coalescence from f0, in units of the total mass
+    (5/256 eta^-1 (pi M f0)^(-8/3)); a cost estimate for ordering the queue."""
+    m1, m2, f0 = params[:, 0], params[:, 1], params[:, 4]
+    M = m1 + m2
+    eta = m1 * m2 / (M * M)
+    x = math.pi * M * MTSUN_SI * f0
+    return (5.0 / 256.0) / eta * x.pow(-8.0 / 3.0)
+
+
+def longest_first(params: torch.Tensor) -> torch.Tensor:
+    """Queue order for the persistent integrator: longest estimated trajectory first."""
+    return torch.argsort(chirp_duration_M(params), descending=True).to(torch.int32)
+
+
+class WaveformLikelihood:
+    """Batched SEOBNR aligned-spin waveform + white-noise likelihood on one GPU.
+
+    max_batch   binaries per call
+    max_steps   trajectory rows per binary (the reference's max_step, raised)
+    modes       list of (l, m), subset of [(2,2), (2,1), (3,3), (4,4), (5,5)]
+    max_samples samples of the data / uniform time grid
+    """
+
+    def __init__(self, max_batch: int, max_steps: int = 20000, modes=((2, 2),), max_samples: int = 8192,
+                 device="cuda", options: _lib.EobOptions | None = None):
+        if not torch.cuda.is_available():
+            raise _lib.EOBError("no CUDA device: the EOB path runs only on the GPU")
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.max_batch, self.max_steps, self.max_samples = int(max_batch), int(max_steps), int(max_samples)
+        self.modes = [tuple(m) for m in modes]
+        self.max_modes = max(1, len(self.modes))
+        nbytes = self.lib.eob_workspace_bytes(self.max_batch, self.max_steps, self.max_modes, self.max_samples)
+        if nbytes == 0:
+            raise _lib.EOBError("invalid workspace capacities")
+        self.ws_bytes = int(nbytes)
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+        self.options = options if options is not None else _lib.default_options()
+        self.ells = (ctypes.c_int * 5)(*[l for l, _ in self.modes])
+        self.mms = (ctypes.c_int * 5)(*[m for _, m in self.modes])
+        self.last_B = 0
+
+    def run(self, params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, order: torch.Tensor | None = None,
+            lnl: torch.Tensor | None = None, status: torch.Tensor | None = None, stream=None):
+        """lnL for every binary of params[B, 5] (m1, m2 [Msun], chi1, chi2, f0 [Hz])."""
+        B = int(params.shape[0])
+        assert params.is_cuda and params.dtype == torch.float64 and params.is_contiguous()
+        assert data.is_cuda and data.dtype == torch.float64 and data.is_contiguous()
+        N = int(data.shape[0])
+        if lnl is None:
+            lnl = torch.empty(B, dtype=torch.float64, device=self.device)
+        if status is None:
+            status = torch.empty(B, dtype=torch.int32, device=self.device)
+        if order is None:
+            order = longest_first(params)
+        rc = self.lib.eob_waveform_lnl(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps, self.max_modes,
+                                       self.max_samples, _ptr(params), _ptr(order), B, self.ells, self.mms,
+                                       len(self.modes), float(dt), _ptr(data), N, float(amp),
+                                       ctypes.byref(self.options), _ptr(lnl), _ptr(status), _stream_handle(stream))
+        _lib.check(rc, "eob_waveform_lnl")
+        self.last_B = B
+        return lnl, status
+
+    def strain(self, params: torch.Tensor, dt: float, n_samples: int, order: torch.Tensor | None = None,
+               status: torch.Tensor | None = None, stream=None):
+        """Complex strain sum_lm h_lm(t_k), k < n_samples, per binary: complex128 [B, n_samples]."""
+        B = int(params.shape[0])
+        assert params.is_cuda and params.dtype == torch.float64 and params.is_contiguous()
+        out = torch.empty((B, n_samples, 2), dtype=torch.float64, device=self.device)
+        if status is None:
+            status = torch.empty(B, dtype=torch.int32, device=self.device)
+        if order is None:
+            order = longest_first(params)
+        rc = self.lib.eob_waveform_strain(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps,
+                                          self.max_modes, self.max_samples, _ptr(params), _ptr(order), B, self.ells,
+                                          self.mms, len(self.modes), float(dt), int(n_samples),
+                                          ctypes.byref(self.options), _ptr(out), _ptr(status),
+                                          _stream_handle(stream))
+        _lib.check(rc, "eob_waveform_strain")
+        self.last_B = B
+        return torch.view_as_complex(out), status
+
+    # ---- inspection of the last run (tests, API mirror) -----------------
+    def views(self) -> _lib.EobViews:
+        v = _lib.EobViews()
+        _lib.check(self.lib.eob_workspace_views(_ptr(self.ws), self.max_batch, self.max_steps, self.max_modes,
+                                                self.max_samples, ctypes.byref(v)), "eob_workspace_views")
+        return v
+
+    def _dev_array(self, addr, count, dtype):
+        """A torch view of `count` elements at a device address inside the workspace."""
+        base = self.ws.data_ptr()
+        off = int(addr) - base
+        esize = torch.empty(0, dtype=dtype).element_size()
+        assert 0 <= off and off + count * esize <= self.ws_bytes
+        return self.ws[off:off + count * esize].view(dtype)
+
+    def trajectories(self):
+        """(nsteps[B], npts[B], status[B], list of (t [M], y[L, 4])) of the last run (host numpy)."""
+        torch.cuda.synchronize()
+        v = self.views()
+        B = self.last_B
+        nsteps = self._dev_array(v.nsteps, B, torch.int32).cpu().numpy()
+        npts = self._dev_array(v.npts, B, torch.int32).cpu().numpy()
+        status = self._dev_array(v.status, B, torch.int32).cpu().numpy()
+        traj = self._dev_array(v.traj, B * self.max_steps * 5, torch.float64).view(B if B else 1, self.max_steps, 5)
+        out = []
+        for b in range(B):
+            L = int(nsteps[b])
+            t = traj[b, :L].cpu().numpy()
+            out.append((t[:, 0].copy(), t[:, 1:].copy()))
+        return nsteps, npts, status, out
+
+    def initial_conditions(self):
+        """(r0, pphi0, pr0) per binary of the last run."""
+        torch.cuda.synchronize()
+        v = self.views()
+        traj = self._dev_array(v.traj, self.last_B * self.max_steps * 5, torch.float64).view(-1, self.max_steps, 5)
+        first = traj[:, 0].cpu().numpy()
+        return np.stack([first[:, 1], first[:, 4], first[:, 3]], axis=1)

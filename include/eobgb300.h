@@ -1,0 +1,183 @@
+/* eobgb300.h -- C ABI of the GB300-native EOB waveform + likelihood path.
+ *
+ * A drop-in native layer for the batched SEOBNR effective-one-body path of
+ * mikekatz04/EOBGPU.  Every entry point takes plain device pointers and
+ * sizes, an explicit cudaStream_t, allocates nothing, and returns an int
+ * status (0 = success, see EOB_E_* below) instead of exiting the process as the
+ * reference's gpuErrchk does (include/global.h:13-20).  Calls are asynchronous
+ * on the given stream; the reference synchronises after every launch.
+ *
+ * Array layouts follow the reference's Cython layer (src/eob.pyx,
+ * src/dopr853.pyx, src/tdinterp.pyx): state arg[4][n] = (r, phi, pr, pphi),
+ * additionalArgs[80][n] = (m1, m2, chi1, chi2, omega, K, d5, dSO, dSS,
+ * h22_calib, then Re/Im of the 35 Newtonian prefixes (l = 2..8, m = 1..l)).
+ */
+#ifndef EOBGB300_H
+#define EOBGB300_H
+
+#include <stddef.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define EOB_OK 0
+#define EOB_E_ARG 1        /* invalid argument / capacity exceeded */
+#define EOB_E_CUDA 2       /* a CUDA runtime call failed */
+#define EOB_E_CTX 3        /* context not initialised */
+
+/* per-binary status bits of the fused pipeline */
+#define EOB_ST_IC_NOCONV 1     /* (r0, pphi0) Newton did not converge */
+#define EOB_ST_MAXSTEP 2       /* trajectory hit the row capacity (max_step) */
+#define EOB_ST_NAN 4           /* non-finite state or error estimate */
+#define EOB_ST_TRIES 8         /* step-attempt limit reached (no progress) */
+#define EOB_ST_SHORT 16        /* too few rows for the step-back restart or the spline */
+#define EOB_ST_STOP_REJECT 32  /* first step of a pass rejected (reference stops there) */
+
+typedef struct eob_options {
+    double rtol, atol;      /* DOPR853 tolerances; reference: 1e-12, 1e-12 (src/DOPR853.cu:7-8) */
+    double h_init;          /* first step [M]; reference 0.01 (eob/new_Dormand_horiz.py:527-531) */
+    double step_back;       /* restart offset [M]; reference 10 (eob/seobnrv4phm.py:2072) */
+    double fine_step;       /* fixed fine step [M]; reference 0.05 */
+    int ic_mode;            /* 0: reference-effective p_r0, 1: physical (exact Hessian) */
+    int precision;          /* 0: FP64 synthesis + lnL, 1: mixed (FP32 amplitude/sincos, compensated sum) */
+    int block;              /* integrator threads per block (0 = default) */
+    int grid;               /* integrator blocks (0 = one wave of resident blocks) */
+    long long max_tries;    /* step attempts per pass before giving up (0 = 2 * max_steps + 100) */
+} eob_options;
+
+void eob_options_default(eob_options *o);
+
+/* ---------------------------------------------------------------------------
+ * Fused path: parameters -> lnL for a batch (no counterpart as one call in the
+ * reference; replaces SEOBNRv4PHM.__call__ + BBHWaveformTD's mode sum and its
+ * likelihood, eob/seobnrv4phm.py:2628-2726, 636-721).
+ * params[B][5] = (m1, m2 [Msun], chi1z, chi2z, f0 [Hz]); data[N];
+ * lnl[B] = -1/2 sum_{k<N} (data_k - amp Re sum_lm h_lm(t_k))^2 with h = 0
+ * past each binary's last sample; status[B] per-binary EOB_ST_* bits.
+ * order[B] (may be NULL) is the order in which the persistent integrator
+ * takes binaries from its queue.
+ */
+size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples);
+int eob_waveform_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                     int max_samples, const double *params, const int *order, int B, const int *ells,
+                     const int *mms, int K, double dt, const double *data, int N, double amp,
+                     const eob_options *opt, double *lnl, int *status, cudaStream_t stream);
+
+/* The same path in two phases, for callers that inspect per-binary results
+ * between them (trajectory rows, sample counts; eob_workspace_views):
+ * eob_prepare runs setup, initial conditions, the integrator, the multipoles
+ * on the trajectory and the splines; eob_synth_lnl / eob_synth_strain then
+ * evaluate the splines on the uniform grid t_k = k dt of each binary.  The
+ * synth calls must get the same B, K, modes and dt as the prepare call. */
+int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
+                const double *params, const int *order, int B, const int *ells, const int *mms, int K, double dt,
+                const eob_options *opt, int *status, cudaStream_t stream);
+int eob_synth_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                  int max_samples, int B, const int *mms, int K, double dt, const double *data, int N, double amp,
+                  double *lnl, int *status, cudaStream_t stream);
+/* per_mode = 0: out[B][N] complex = sum_lm h_lm(t_k), zero past each binary's last sample;
+ * per_mode = 1: out[B][K][N] complex per mode with t_k clamped to each binary's last sample
+ * (the uniform-grid modes of SEOBNRv4PHM.__call__, eob/seobnrv4phm.py:2336-2372). */
+int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                     int max_samples, int B, const int *mms, int K, double dt, int N, int per_mode, double *out,
+                     int *status, cudaStream_t stream);
+
+/* Same pipeline, writing the summed strain instead of the likelihood:
+ * strain[B][N] complex (re, im interleaved) = sum_lm h_lm(t_k) on the grid
+ * t_k = k dt from each binary's start, zero past its last sample (the
+ * mode sum of BBHWaveformTD, eob/seobnrv4phm.py:715-721; "geocenter_td"). */
+int eob_waveform_strain(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                        int max_samples, const double *params, const int *order, int B, const int *ells,
+                        const int *mms, int K, double dt, int N, const eob_options *opt, double *strain, int *status,
+                        cudaStream_t stream);
+
+/* Device pointers into a workspace after eob_waveform_lnl: trajectories
+ * traj[b][row][5] = (t [M], r, phi, pr, pphi), nsteps[b] rows each;
+ * npts[b] uniform-grid samples of each binary's waveform. */
+typedef struct eob_views {
+    double *traj;
+    int *nsteps;
+    int *status;
+    int *npts;
+    long long *row_off;
+    double *tin;          /* knot times [M], packed by row_off */
+    double *spline_y;     /* [nsubs][rows]: phi, then Re/Im of h_lm e^{i m phi} per mode */
+    double *spline_c1, *spline_c2, *spline_c3;
+    int row_capacity;     /* max_steps */
+    long long rows_capacity;
+    int nsubs;
+} eob_views;
+int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
+                        eob_views *out);
+
+/* ---------------------------------------------------------------------------
+ * Reference-shaped entry points (src/eob.pyx, src/dopr853.pyx, src/tdinterp.pyx)
+ */
+
+/* src/eob.pyx:79 evaluate_Ham_align_AD -> src/EOB.cu:127 evaluate_Ham_align_AD_wrap */
+int eob_evaluate_ham(double *out, const double *r, const double *phi, const double *pr, const double *pphi,
+                     const double *m_1, const double *m_2, const double *chi_1, const double *chi_2, double K,
+                     double d5, double dSO, double dSS, int numSys, cudaStream_t stream);
+/* src/eob.pyx:61 grad_Ham_align_AD -> src/EOB.cu:242 grad_Ham_align_AD_wrap */
+int eob_grad_ham(const double *arg, double *grad_out, const double *additionalArgs, int numSys, cudaStream_t stream);
+/* src/eob.pyx:70 hessian_Ham_align_AD -> src/EOB.cu:391 hessian_Ham_align_AD_wrap (exact d2H/dr2) */
+int eob_hessian_ham(const double *arg, double *hessian_out, const double *additionalArgs, int numSys,
+                    cudaStream_t stream);
+/* src/eob.pyx:94 IC_cons -> src/EOB.cu:451 IC_cons_wrap */
+int eob_ic_cons(double *res, const double *x, double *args, const double *additionalArgs, double *grad_out,
+                int numSys, cudaStream_t stream);
+/* src/eob.pyx:51 root_find_all -> src/EOB.cu:3033 root_find_all_wrap (n = 2, num_args = 4) */
+int eob_root_find_all(double *xOut, const double *x0In, const double *argsIn, const double *additionalArgsIn,
+                      int max_iter, double err, int numBinAll, int n, int num_args, int num_add_args,
+                      cudaStream_t stream);
+
+/* SEOBNRv5 class (src/eob.pyx:106-255, src/EOB.cu:3343-3496) as a context:
+ * per-binary coefficient tables live in caller memory of
+ * eob_ctx_bytes(numSys) bytes. */
+size_t eob_ctx_bytes(int numSys);
+/* src/eob.pyx:118 update_information -> src/EOB.cu:3355; prefixes (re, im) interleaved, [35][numSys] */
+int eob_ctx_update_information(void *ctx, const double *m1, const double *m2, const double *eta, const double *tplspin,
+                               const double *chi_S, const double *chi_A, int use_hm, int numSys,
+                               cudaStream_t stream);
+/* src/eob.pyx:158 ODE_Ham_align_AD -> src/EOB.cu:3486 */
+int eob_ctx_ode(const void *ctx, const double *x, const double *arg, double *k, const double *additionalArgs,
+                int numSys, const int *hCoeffs_index, cudaStream_t stream);
+/* src/eob.pyx:147 RR_force -> src/EOB.cu:3385 */
+int eob_ctx_rr_force(const void *ctx, double *force_out, double *grad_out, const double *args,
+                     const double *additionalArgs, int numSys, const int *hCoeffs_index, cudaStream_t stream);
+/* src/eob.pyx:169 root_find_scalar_all -> src/EOB.cu:3398 (ic_mode as eob_options) */
+int eob_ctx_root_find_scalar_all(const void *ctx, double *pr_res, const double *start_bounds, const double *argsIn,
+                                 const double *additionalArgsIn, int max_iter, double err, int numBinAll,
+                                 int num_args, int num_add_args, int ic_mode, cudaStream_t stream);
+/* src/eob.pyx:203 EOBGetSpinFactorizedWaveform -> src/EOB.cu:3423; out and newtonian_prefix complex interleaved */
+int eob_ctx_waveform(const void *ctx, double *out, const double *r, const double *phi, const double *pr,
+                     const double *pphi, const double *v, const double *Hreal, const double *eta,
+                     const double *vPhiInput, int l, int m, const double *newtonian_prefix, double h22_calib,
+                     int numSys, int traj_length, const int *hCoeffs_index, cudaStream_t stream);
+
+/* src/dopr853.pyx:67 dormandPrinceSteps -> src/DOPR853.cu:357 (one fused launch) */
+int eob_dopr853_steps(const double *x, double *xCurrent, const double *solOld, const double *h, double *arg,
+                      const double *additionalArgs, double *k1, double *k2, double *k3, double *k4, double *k5,
+                      double *k6, double *k7, double *k8, double *k9, double *k10, double *ak_term_buffer, int nargs,
+                      int numEq, int num_add_args, const void *ctx, const int *hCoeffs_index, cudaStream_t stream);
+/* src/dopr853.pyx:139 error -> src/DOPR853.cu:620 */
+int eob_dopr853_error(double *err, const double *solOld, double *solNew, const double *h, const double *k1,
+                      const double *k2, const double *k3, const double *k6, const double *k7, const double *k8,
+                      const double *k9, const double *k10, int numEq, int nargs, cudaStream_t stream);
+/* src/dopr853.pyx:187 controllerSuccess -> src/DOPR853.cu:764 (bool arrays as bytes) */
+int eob_dopr853_controller(unsigned char *flagSuccess, const double *err, double *errOld,
+                           unsigned char *previousReject, double *h, const double *x, int numEq, int nargs,
+                           cudaStream_t stream);
+
+/* src/tdinterp.pyx:21 interpolate_TD_wrap -> src/interpolate.cu:269; c1/c2/c3 overwrite
+ * upper_diag/diag/lower_diag as in the reference */
+int eob_interpolate_td(const double *t_arr, const double *propArrays, double *B, double *upper_diag, double *diag,
+                       double *lower_diag, const int *lengths, int numBinAll, int nsubs, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

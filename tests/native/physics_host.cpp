@@ -1,0 +1,57 @@
+// Host build of the product's device physics (eobgpu_gb300/csrc/physics/)
+// for CPU tests: the same headers the CUDA kernels compile, exercised
+// through a small extern "C" surface and compared with the oracle.
+#include "../../eobgpu_gb300/csrc/physics/fac_coeffs.h"
+#include "../../eobgpu_gb300/csrc/physics/ham_coeffs.h"
+#include "../../eobgpu_gb300/csrc/physics/ham_eval.h"
+#include "../../eobgpu_gb300/csrc/physics/flux_eval.h"
+
+extern "C" {
+
+// state[4][n], add[80][n] (reference layout); out: H, dHdr, dHdpr, dHdL, omega_c per point
+void phys_ham(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, add[i], add[n + i], add[2 * n + i], add[3 * n + i], add[5 * n + i], add[6 * n + i],
+                              add[7 * n + i], add[8 * n + i]);
+        eob::HamEval e;
+        eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
+        out[5 * i + 0] = e.H; out[5 * i + 1] = e.dHdr; out[5 * i + 2] = e.dHdpr; out[5 * i + 3] = e.dHdL;
+        out[5 * i + 4] = e.omega_c;
+    }
+}
+
+// ODE right-hand side with coefficient tables built for each point's binary
+void phys_rhs(const double *st, const double *add, int n, double *k)
+{
+    for (int i = 0; i < n; ++i) {
+        const double m1 = add[i], m2 = add[n + i], c1 = add[2 * n + i], c2 = add[3 * n + i];
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, m1, m2, c1, c2, add[5 * n + i], add[6 * n + i], add[7 * n + i], add[8 * n + i]);
+        const double eta = m1 * m2 / ((m1 + m2) * (m1 + m2));
+        const double chiS = 0.5 * (c1 + c2), chiA = 0.5 * (c1 - c2);
+        const double tpl = (1.0 - 2.0 * eta) * chiS + (m1 - m2) / (m1 + m2) * chiA;
+        static eob::FacCoeffs fc;
+        eob::fac_coeffs_build(&fc, 1, m1, m2, eta, tpl, chiS, chiA);
+        double pre_re[35], pre_im[35];
+        for (int j = 0; j < 35; ++j) { pre_re[j] = add[(10 + 2 * j) * n + i]; pre_im[j] = add[(11 + 2 * j) * n + i]; }
+        static eob::FluxTable t;
+        eob::flux_table_build(&t, fc, pre_re, pre_im, add[9 * n + i], h.nu);
+        const double y[4] = {st[i], st[n + i], st[2 * n + i], st[3 * n + i]};
+        double kk[4];
+        eob::eob_rhs(h, t, y, kk);
+        for (int q = 0; q < 4; ++q) k[q * n + i] = kk[q];
+    }
+}
+
+// Newtonian prefixes of one binary, interleaved (re, im) x 35
+void phys_prefixes(double m1, double m2, double *out)
+{
+    for (int l = 2; l <= 8; ++l)
+        for (int m = 1; m <= l; ++m) {
+            const int i = eob::lm_index(l, m);
+            eob::newton_prefix(m1, m2, l, m, &out[2 * i], &out[2 * i + 1]);
+        }
+}
+}

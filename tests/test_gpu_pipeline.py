@@ -1,0 +1,88 @@
+"""The fused CUDA path against the reference's golden outputs and the oracle
+(configuration 1 and variations), through the C ABI."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def cfg1_run(torch_cuda, golden):
+    torch = torch_cuda
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    c = golden["config1"]
+    P = torch.tensor(c["params"], dtype=torch.float64, device="cuda")
+    d = torch.tensor(c["data"], dtype=torch.float64, device="cuda")
+    wl = WaveformLikelihood(max_batch=len(P), max_steps=20000, modes=[(2, 2)], max_samples=int(c["N"]))
+    lnl, st = wl.run(P, d, float(c["dt"]), float(c["amp"]))
+    torch.cuda.synchronize()
+    return wl, lnl.cpu().numpy(), st.cpu().numpy(), c
+
+
+def test_config1_status_ok(cfg1_run):
+    _, lnl, st, _ = cfg1_run
+    assert np.all(st == 0), st
+    assert np.all(np.isfinite(lnl))
+
+
+def test_config1_initial_conditions(cfg1_run):
+    wl, _, _, c = cfg1_run
+    ic = wl.initial_conditions()
+    np.testing.assert_allclose(ic[:, :2], c["ic"][:, :2], rtol=1e-11)
+    assert np.all(np.abs(ic[:, 2]) < 2e-12)
+
+
+def test_config1_trajectory_rows(cfg1_run):
+    """Same number of trajectory rows and waveform samples as the reference;
+    rows are not compared one by one because adaptive step sizes differ at the
+    1e-5 level between implementations (the waveform comparison below is the
+    size-independent check)."""
+    wl, _, _, c = cfg1_run
+    nsteps, npts, st, trajs = wl.trajectories()
+    np.testing.assert_array_equal(nsteps, c["nsteps"])
+    np.testing.assert_array_equal(npts, c["npts"])
+    for b, (t, y) in enumerate(trajs):
+        L = nsteps[b]
+        assert t[0] == 0.0 and np.all(np.diff(t) > 0)
+        # fixed 0.05 M steps at the end of the fine pass
+        np.testing.assert_allclose(np.diff(t[-20:]), 0.05, rtol=1e-12)
+        assert abs(t[-1] - c["traj_t"][b, L - 1]) < 0.05
+
+
+def test_config1_strain_vs_reference(cfg1_run, torch_cuda):
+    """Strain on the uniform grid vs the reference: |h| and the phase at the
+    peak of |h| (FP64 bounds: relative amplitude 1e-8 of the peak, 1e-5 rad)."""
+    torch = torch_cuda
+    wl, _, _, c = cfg1_run
+    P = torch.tensor(c["params"][:2], dtype=torch.float64, device="cuda")
+    h, st = wl.strain(P, float(c["dt"]), int(c["N"]))
+    h = h.cpu().numpy()
+    for b in range(2):
+        hr = c[f"h_{b}"]
+        n = int(c["npts"][b])
+        assert np.all(h[b, n:] == 0)
+        peak = np.argmax(np.abs(hr[:n]))
+        assert np.max(np.abs(h[b, :n] - hr[:n])) < 1e-8 * np.abs(hr[peak])
+        dphi = np.angle(h[b, peak] / hr[peak])
+        assert abs(dphi) < 1e-5, dphi
+
+
+def test_config1_lnl_vs_reference(cfg1_run):
+    _, lnl, _, c = cfg1_run
+    rel = np.abs(lnl / c["lnl"] - 1)
+    assert np.all(rel < 1e-9), rel
+
+
+def test_config1_lnl_vs_oracle(cfg1_run, oracle):
+    _, lnl, _, c = cfg1_run
+    for b in range(len(lnl)):
+        r = oracle.lnl_one(c["params"][b], float(c["dt"]), int(c["N"]), [(2, 2)], c["data"], float(c["amp"]))
+        assert abs(lnl[b] / r["lnl"] - 1) < 1e-9, (b, lnl[b], r["lnl"])
