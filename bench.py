@@ -1,0 +1,403 @@
+"""Benchmark of the batched EOB waveform + likelihood path on GB300.
+
+Default workload: the ragged-batching configuration -- 1024 aligned-spin
+binaries, M ~ U[20, 200] Msun, q ~ U[1, 8], chi ~ U[-0.9, 0.9],
+f0 ~ U[10, 20] Hz, (2,2) mode, dt = 1/2048 s, N = 2^17 samples, white-noise
+data with one injection at SNR 30, FP64 throughout.  A step is one pass of the
+whole path (parameters -> lnL) over the batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference] [--config 1|2|3|5]
+
+Under torchrun (N > 1) every rank runs its own batch (replicas: the path has
+no exchange step); value = all binaries of all ranks / max-over-ranks time.
+`--impl reference` times the CPU restatement of the reference path (the
+oracle) on the host cores.  Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from eobgpu_gb300 import workload  # noqa: E402
+
+METRIC = "waveform+lnL evals/s"
+# FP64 floating-point operations of one right-hand-side evaluation of the
+# integrator: hardware census (ncu DADD + DMUL + 2 DFMA thread instructions of
+# k_integrate divided by the lane-RHS count) -- profiles/k_integrate_fp64_census.md
+F_RHS = None  # filled from the census file at import time below
+
+CENSUS = os.path.join(ROOT, "profiles", "k_integrate_fp64_census.md")
+
+
+def _census_flops():
+    try:
+        with open(CENSUS) as f:
+            for line in f:
+                if line.startswith("F_RHS_FLOPS"):
+                    return float(line.split("=")[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+F_RHS = _census_flops()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("EOB_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        try:
+            self.f.close()
+        except Exception:
+            pass
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) >= 9:
+                        rows.append(p)
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = np.array([float(r[1]) for r in rows])
+        mx = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].lower() == "active"})
+        busy = sm[sm > 0.5 * np.max(sm)] if len(sm) else sm
+        return {"sm_mhz": float(np.median(busy)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def make_inputs(cfg, stream_seed, device, max_steps):
+    """Seeded parameters of the configuration and data built from the injection."""
+    import torch
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    params = workload.draw_params(cfg, stream=stream_seed)
+    inj = workload.injection_params(cfg)
+    wl = WaveformLikelihood(1, max_steps, list(cfg.modes), cfg.n_samples, device=device)
+    h, st = wl.strain(torch.tensor(inj[None, :], device=device), cfg.dt, cfg.n_samples)
+    torch.cuda.synchronize()
+    data, amp = workload.make_data(h[0].real.cpu().numpy(), cfg.n_samples, cfg.index)
+    del wl
+    return params, data, amp
+
+
+def _oracle_worker(args):
+    p, dt, N, modes, data, amp, max_step = args
+    from oracle.oracle import Oracle
+    o = Oracle()
+    return o.lnl_one(p, dt, N, modes, data, amp, max_step=max_step)["lnl"]
+
+
+def cpu_time(params, cfg, data, amp, max_step, cores):
+    """Wall time of the oracle (CPU restatement of the reference path) over params on `cores` processes."""
+    import multiprocessing as mp
+    jobs = [(p, cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, max_step) for p in params]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_worker, jobs[:cores])  # start-up and first-call costs outside the timing
+        t0 = time.perf_counter()
+        out = pool.map(_oracle_worker, jobs, chunksize=1)
+        t1 = time.perf_counter()
+    return t1 - t0, np.array(out)
+
+
+def cpu_sample(params, n):
+    """Deterministic bounded sample: every k-th binary."""
+    step = max(1, len(params) // n)
+    return params[::step][:n]
+
+
+def run_reference(args, cfg, ws, rank):
+    """The reference arm: CPU restatement of the reference path on all host cores."""
+    if rank != 0:
+        return None
+    from oracle import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    params = workload.draw_params(cfg, stream=0)
+    # data from the oracle's own injection (the reference arm runs without a GPU)
+    inj = orc.Oracle().lnl_one(workload.injection_params(cfg), cfg.dt, cfg.n_samples, list(cfg.modes),
+                               np.zeros(cfg.n_samples), 1.0, max_step=args.max_steps, want_detail=True)
+    data, amp = workload.make_data(inj["h"].real, cfg.n_samples, cfg.index)
+    n = args.cpu_sample
+    sample = cpu_sample(params, n)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_time(sample[:cores], cfg, data, amp, args.max_steps, cores)
+    times = []
+    for _ in range(args.steps):
+        t, _ = cpu_time(sample, cfg, data, amp, args.max_steps, cores)
+        times.append(t)
+    tt = float(np.sum(times))
+    value = len(sample) * args.steps / tt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
+            "config": config_block(cfg, args, extra={"sample": len(sample)}),
+            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(sample)} of {cfg.batch} binaries (every {max(1, cfg.batch // n)}th), "
+                                       f"per step"},
+            "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def config_block(cfg, args, extra=None):
+    d = {"workload": f"config {cfg.index}: {cfg.name}", "batch": args.batch or cfg.batch,
+         "total_mass_msun": list(cfg.total_mass), "mass_ratio": list(cfg.mass_ratio), "chi": list(cfg.chi),
+         "f0_hz": list(cfg.f0), "modes": [list(m) for m in cfg.modes], "dt_s": cfg.dt, "n_samples": cfg.n_samples,
+         "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12, "queue": "longest first",
+         "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def census(args):
+    """Every lane integrates the same binary, so the launch's lane-RHS count is
+    exact; run under ncu with -k regex:k_integrate -s 3 -c 1 and divide the
+    FP64 instruction census by rhs_all_lanes."""
+    import torch
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    cfg = workload.CONFIGS[1]
+    p = workload.draw_params(cfg, batch=1, stream=0)
+    P = torch.tensor(np.repeat(p, 128, axis=0), device="cuda")
+    wl = WaveformLikelihood(128, 4000, [(2, 2)], cfg.n_samples)
+    for _ in range(4):
+        wl.prepare(P, cfg.dt, stages=3)
+    torch.cuda.synchronize()
+    print(json.dumps({"census": wl.counters()}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 5])
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--max-steps", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=96)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--census", action="store_true",
+                    help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
+    args = ap.parse_args()
+    cfg = workload.CONFIGS[args.config]
+    if args.batch:
+        cfg = workload.Config(**{**cfg.__dict__, "batch": args.batch})
+    if not args.max_steps:
+        args.max_steps = {1: 4000, 2: 6000, 3: 4000, 5: 16000}[args.config]
+    args.warmup = max(3, args.warmup)
+    if args.census:
+        census(args)
+        return
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        line = run_reference(args, cfg, int(os.environ.get("WORLD_SIZE", "1")), rank)
+        if line is not None:
+            print(json.dumps(line))
+        return
+    ws, rank, local = dist_init()
+
+    if args.impl == "reference":
+        line = run_reference(args, cfg, ws, rank)
+        if line is not None:
+            print(json.dumps(line))
+        return
+
+    import torch
+    from eobgpu_gb300.pipeline import WaveformLikelihood, longest_first, chirp_duration_M
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    params, data, amp = make_inputs(cfg, rank, device, args.max_steps)
+    B = params.shape[0]
+    K = len(cfg.modes)
+    wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device)
+    P = torch.tensor(params, device=device)
+    D = torch.tensor(data, device=device)
+    order = longest_first(P)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    def step():
+        return wl.run(P, D, cfg.dt, amp, order=order)
+
+    for _ in range(args.warmup):
+        lnl, st = step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (value)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            lnl, st = step()
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        barrier(ws)
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        # ---- end to end through the public API with host buffers
+        params_h = torch.tensor(params).pin_memory()
+        order_h = order.cpu().pin_memory()
+        lnl_h = torch.empty(B, dtype=torch.float64).pin_memory()
+        st_h = torch.empty(B, dtype=torch.int32).pin_memory()
+        ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev2[i][0].record()
+            Pd = params_h.to(device, non_blocking=True)
+            Od = order_h.to(device, non_blocking=True)
+            l_d, s_d = wl.run(Pd, D, cfg.dt, amp, order=Od)
+            lnl_h.copy_(l_d, non_blocking=True)
+            st_h.copy_(s_d, non_blocking=True)
+            ev2[i][1].record()
+        torch.cuda.synchronize()
+        e2e_ms = [a.elapsed_time(b) for a, b in ev2]
+    clocks = clk.summary()
+    t_dev = max_over_ranks(float(np.sum(step_ms)), ws, device)
+    t_e2e = max_over_ranks(float(np.sum(e2e_ms)), ws, device)
+    value = B * ws * args.steps / (t_dev / 1e3)
+    e2e_value = B * ws * args.steps / (t_e2e / 1e3)
+    status = st.cpu().numpy()
+
+    # ---- stage timing and roofline of the integrator (one more untimed step)
+    s_ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    flush.fill_(1.0)
+    s_ev[0].record()
+    wl.prepare(P, cfg.dt, order=order, stages=1)
+    s_ev[1].record()
+    wl.prepare(P, cfg.dt, order=order, stages=2)
+    s_ev[2].record()
+    wl.prepare(P, cfg.dt, order=order, stages=4)
+    s_ev[3].record()
+    wl.synth_lnl(B, D, cfg.dt, amp)
+    s_ev[4].record()
+    torch.cuda.synchronize()
+    stage_ms = {"setup_ic": s_ev[0].elapsed_time(s_ev[1]), "integrate": s_ev[1].elapsed_time(s_ev[2]),
+                "modes_splines": s_ev[2].elapsed_time(s_ev[3]), "synth_lnl": s_ev[3].elapsed_time(s_ev[4])}
+    cnt = wl.counters()
+    # FP64 peak of this device, measured
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    pk_out = torch.empty(nsm * 8 * 256, dtype=torch.float64, device=device)
+    iters = 4096
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        wl.lib.eob_fp64_probe(pk_out.data_ptr(), nsm * 8, 256, iters, torch.cuda.current_stream().cuda_stream)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    fp64_peak = 2.0 * 8 * iters * nsm * 8 * 256 / (best / 1e3) / 1e12
+    roof = None
+    if F_RHS:
+        achieved = F_RHS * cnt["rhs_binaries"] / (stage_ms["integrate"] / 1e3) / 1e12
+        roof = {"kernel": "k_integrate", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "measured live: FP64 DFMA probe (eob_fp64_probe), burst",
+                "work": f"{F_RHS:.0f} FP64 FLOP per RHS x {cnt['rhs_binaries']} RHS evaluations",
+                "lane_occupancy": cnt["rhs_binaries"] / max(1, cnt["rhs_all_lanes"])}
+
+    line = None
+    if rank == 0:
+        cpu_base = None
+        if not args.no_cpu_baseline:
+            cores = os.cpu_count() or 1
+            sample = cpu_sample(params, args.cpu_sample)
+            t, _ = cpu_time(sample, cfg, data, amp, args.max_steps, cores)
+            cpu_base = {"value": len(sample) / t, "unit": "evals/s", "cores": cores, "kind": "port",
+                        "sample": f"{len(sample)} of {B} binaries (every {max(1, B // args.cpu_sample)}th)"}
+        launches_per_step = 8  # setup, integrate, scan_rows, modes, spline, scan_chunks, synth, finalize
+        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
+                "config": config_block(cfg, args),
+                "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(B * 5 * 8 + B * 4),
+                        "d2h_bytes_per_step": int(B * 8 + B * 4)},
+                "roofline": roof, "cpu_baseline": cpu_base, "clocks": clocks,
+                "gpu_launches": launches_per_step * args.steps,
+                "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+                "stages_ms": stage_ms, "fp64_peak_tflops": fp64_peak,
+                "status_ok": int(np.sum(status == 0)), "rows": cnt["rows"]}
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

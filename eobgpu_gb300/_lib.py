@@ -21,7 +21,7 @@ c_ll = ctypes.c_longlong
 class EobOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("h_init", c_double), ("step_back", c_double),
                 ("fine_step", c_double), ("ic_mode", c_int), ("precision", c_int), ("block", c_int),
-                ("grid", c_int), ("max_tries", c_ll)]
+                ("grid", c_int), ("max_tries", c_ll), ("lanes_per_binary", c_int), ("pad_", c_int)]
 
 
 class EobViews(ctypes.Structure):
@@ -42,10 +42,14 @@ _SIGS = {
                                     c_double, c_int, ctypes.POINTER(EobOptions), _P, _P, _P]),
     "eob_prepare": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, _P, _P, c_int, _P, _P, c_int, c_double,
                             ctypes.POINTER(EobOptions), _P, _P]),
+    "eob_prepare_stages": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, _P, _P, c_int, _P, _P, c_int,
+                                   c_double, ctypes.POINTER(EobOptions), c_int, _P]),
     "eob_synth_lnl": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, c_int, _P, c_int, c_double, _P, c_int,
                               c_double, _P, _P, _P]),
     "eob_synth_strain": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, c_int, _P, c_int, c_double, c_int, c_int,
                                  _P, _P, _P]),
+    "eob_workspace_counters": (c_int, [_P, c_int, c_int, c_int, c_int, _P, _P]),
+    "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
     "eob_workspace_views": (c_int, [_P, c_int, c_int, c_int, c_int, ctypes.POINTER(EobViews)]),
     "eob_evaluate_ham": (c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, c_double, c_double, c_double, c_double, c_int,
                                  _P]),

@@ -20,6 +20,8 @@ void eob_options_default(eob_options *o)
     o->block = 0;
     o->grid = 0;
     o->max_tries = 0;
+    o->lanes_per_binary = 0;
+    o->pad_ = 0;
 }
 
 size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples)
@@ -43,9 +45,9 @@ static bool modes_ok(const int *ells, const int *mms, int K, int max_modes)
     return true;
 }
 
-int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
-                const double *params, const int *order, int B, const int *ells, const int *mms, int K, double dt,
-                const eob_options *opt, int *status, cudaStream_t stream)
+int eob_prepare_stages(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                       int max_samples, const double *params, const int *order, int B, const int *ells, const int *mms,
+                       int K, double dt, const eob_options *opt, int stages, cudaStream_t stream)
 {
     WsLayout L;
     if (!workspace || !params || !dims_ok(workspace_bytes, max_batch, max_steps, max_modes, max_samples, &L))
@@ -60,12 +62,21 @@ int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_
     for (int j = 0; j < K; ++j) { a.ells[j] = ells[j]; a.mms[j] = mms[j]; }
     a.dt = dt;
     if (opt) a.opt = *opt; else eob_options_default(&a.opt);
-    a.status_out = status;
     const Ws w = ws_views(workspace, L);
-    cudaError_t e = launch_setup(w, a, stream);
-    if (e == cudaSuccess) e = launch_integrate(w, a, stream);
-    if (e == cudaSuccess) e = launch_prepare_post(w, a, stream);
+    cudaError_t e = cudaSuccess;
+    if (stages & 1) e = launch_setup(w, a, stream);
+    if (e == cudaSuccess && (stages & 2)) e = launch_integrate(w, a, stream);
+    if (e == cudaSuccess && (stages & 4)) e = launch_prepare_post(w, a, stream);
     return e == cudaSuccess ? EOB_OK : EOB_E_CUDA;
+}
+
+int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
+                const double *params, const int *order, int B, const int *ells, const int *mms, int K, double dt,
+                const eob_options *opt, int *status, cudaStream_t stream)
+{
+    (void)status;
+    return eob_prepare_stages(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, params, order,
+                              B, ells, mms, K, dt, opt, 7, stream);
 }
 
 static int synth(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
@@ -134,6 +145,17 @@ int eob_waveform_strain(void *workspace, size_t workspace_bytes, int max_batch, 
     if (rc != EOB_OK) return rc;
     return eob_synth_strain(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, N,
                             0, strain, status, stream);
+}
+
+int eob_workspace_counters(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
+                           unsigned long long *out8, cudaStream_t stream)
+{
+    if (!workspace || !out8) return EOB_E_ARG;
+    const WsLayout L = ws_layout(max_batch, max_steps, max_modes, max_samples);
+    const Ws w = ws_views(workspace, L);
+    cudaError_t e = cudaMemcpyAsync(out8, w.queue, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    return e == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 
 int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,

@@ -50,7 +50,7 @@ EOB_HD WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
     w.traj = o;      o = align256(o + sizeof(double) * kTrajStride * rows);
     w.nsteps = o;    o = align256(o + sizeof(int) * (size_t)Bc);
     w.status = o;    o = align256(o + sizeof(int) * (size_t)Bc);
-    w.queue = o;     o = align256(o + sizeof(unsigned long long) * 4);
+    w.queue = o;     o = align256(o + sizeof(unsigned long long) * 8);
     w.row_off = o;   o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
     w.chunk_off = o; o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
     w.npts = o;      o = align256(o + sizeof(int) * (size_t)Bc);
@@ -71,7 +71,8 @@ struct Ws {
     FacCoeffs *fac;
     double *traj;
     int *nsteps, *status;
-    unsigned long long *queue;  // [0] work queue, [1] total rows, [2] total chunks, [3] sum data^2 (double bits)
+    unsigned long long *queue;  // [0] work queue, [1] total rows, [2] total chunks, [3] sum data^2 (double bits),
+                                // [4] RHS evaluations for binaries, [5] RHS evaluations incl. idle lanes
     long long *row_off, *chunk_off;
     int *npts;
     double *tin, *ys, *cA, *cB, *cC, *cD, *partial;

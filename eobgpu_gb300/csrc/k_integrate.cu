@@ -107,8 +107,16 @@ struct IntArgs {
     long long max_tries;
 };
 
+template <int G>
 __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
 {
+    // G consecutive lanes carry one binary; every lane of the group keeps the
+    // same state (identical arithmetic), the flux multipoles are split over
+    // the group, and only the group leader writes results.
+    const int lane = threadIdx.x & 31;
+    const int sub = lane & (G - 1);
+    const bool leader = (sub == 0);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - sub));
     // per-lane DOPR853 state
     double k[11][4];  // slopes k1..k10 (slot 0 unused)
     double y[4], ynew[4], arg[4];
@@ -117,6 +125,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
     bool prevReject = false, fix = false;
     long long tries = 0;
+    unsigned long long n_useful = 0, n_all = 0;  // RHS evaluations (census for the roofline)
     const BinaryRec *rec = nullptr;
     double *tr = nullptr;
     bool queue_empty = false;
@@ -124,7 +133,9 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
     for (;;) {
         // ------------------------------------------------ bookkeeping
         if (phase == kIdle && !queue_empty) {
-            const unsigned long long slot = atomicAdd(&a.queue[0], 1ull);
+            unsigned long long slot = 0;
+            if (leader) slot = atomicAdd(&a.queue[0], 1ull);
+            if (G > 1) slot = __shfl_sync(gmask, slot, lane - sub);
             if (slot >= (unsigned long long)a.B) {
                 queue_empty = true;
             } else {
@@ -136,8 +147,10 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 step = 0;
                 x = 0.0;
                 for (int q = 0; q < 4; ++q) y[q] = rec->y0[q];
-                tr[0] = 0.0;
-                for (int q = 0; q < 4; ++q) tr[1 + q] = y[q];
+                if (leader) {
+                    tr[0] = 0.0;
+                    for (int q = 0; q < 4; ++q) tr[1 + q] = y[q];
+                }
                 h = a.h_init;
                 hfix = a.h_init;
                 fix = false;
@@ -147,6 +160,8 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         const bool active = (phase != kIdle);
         // all lanes of the warp idle and the queue exhausted: done
         if (__all_sync(0xffffffffu, !active)) break;
+        n_all += leader ? 1ull : 0ull;
+        n_useful += (active && leader) ? 1ull : 0ull;
 
         // ------------------------------------------------ RHS argument
         int out_slot = 1;
@@ -170,7 +185,8 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
 
         // ------------------------------------------------ the one RHS per loop
         double kk[4];
-        eob_rhs(rec->ham, rec->flux, arg, kk);
+        if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
+        else eob_rhs_group<G>(rec->ham, rec->flux, arg, kk, sub);
         if (!active) continue;
 
         // ------------------------------------------------ advance the lane
@@ -241,9 +257,11 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 for (int q = 0; q < 4; ++q) y[q] = ynew[q];
                 x = x + hOld;
                 ++step;
-                double *row = tr + (size_t)step * kTrajStride;
-                row[0] = x;
-                for (int q = 0; q < 4; ++q) row[1 + q] = y[q];
+                if (leader) {
+                    double *row = tr + (size_t)step * kTrajStride;
+                    row[0] = x;
+                    for (int q = 0; q < 4; ++q) row[1 + q] = y[q];
+                }
                 phase = kStopTest;  // next RHS: f(y_new) for the stopping rule and the next k1
                 if (bad) st |= EOB_ST_NAN;
             } else {
@@ -299,8 +317,10 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
             const int S1 = step;
             if (S1 < 2 || (st & (EOB_ST_NAN | EOB_ST_TRIES))) {
                 st |= EOB_ST_SHORT;
-                a.nsteps[b] = S1 + 1;
-                a.status[b] |= st;
+                if (leader) {
+                    a.nsteps[b] = S1 + 1;
+                    a.status[b] |= st;
+                }
                 phase = kIdle;
                 continue;
             }
@@ -326,10 +346,49 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
             continue;
         }
         // pass 2 finished: binary done
-        a.nsteps[b] = step + 1;
-        a.status[b] |= st;
+        if (leader) {
+            a.nsteps[b] = step + 1;
+            a.status[b] |= st;
+        }
         phase = kIdle;
     }
+    if (leader) {
+        atomicAdd(&a.queue[4], n_useful);
+        atomicAdd(&a.queue[5], n_all);
+    }
+}
+
+template <int G>
+cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
+{
+    if (grid <= 0) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<G>, bs, 0);
+        if (per_sm < 1) per_sm = 1;
+        const long long lanes = (long long)a.B * G;
+        const long long need = (lanes + bs - 1) / bs;
+        grid = (int)(need < (long long)nsm * per_sm ? need : (long long)nsm * per_sm);
+        if (grid < 1) grid = 1;
+    }
+    k_integrate<G><<<grid, bs, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// Lanes per binary: enough lanes for about one warp per SM sub-partition,
+// power of two in [1, 32].  One lane per binary is the most efficient use of
+// the FP64 pipe; more lanes per binary shorten each binary's critical path
+// when the batch cannot fill the device.
+int auto_lanes_per_binary(int B)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long long target = (long long)nsm * 4 * 32;
+    int G = 1;
+    while (G < 32 && (long long)B * (G * 2) <= target) G *= 2;
+    return G;
 }
 
 cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
@@ -350,23 +409,19 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
     a.step_back = ra.opt.step_back;
     a.tmax = 1e7 * 1e6;
     a.max_tries = ra.opt.max_tries > 0 ? ra.opt.max_tries : 2LL * w.L.Lc + 100;
-    const int bs = (ra.opt.block > 0 && ra.opt.block <= 256) ? ra.opt.block : 128;
-    int grid = ra.opt.grid;
-    if (grid <= 0) {
-        // enough lanes for every binary, at most one wave of resident blocks
-        int dev = 0, nsm = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate, bs, 0);
-        if (per_sm < 1) per_sm = 1;
-        const int need = (ra.B + bs - 1) / bs;
-        grid = need < nsm * per_sm ? need : nsm * per_sm;
-        if (grid < 1) grid = 1;
-    }
-    cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long), s);
+    const int bs = (ra.opt.block > 0 && ra.opt.block <= 256 && ra.opt.block % 32 == 0) ? ra.opt.block : 128;
+    int G = ra.opt.lanes_per_binary;
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32) G = auto_lanes_per_binary(ra.B);
+    cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long) * 8, s);
     if (e != cudaSuccess) return e;
-    k_integrate<<<grid, bs, 0, s>>>(a);
-    return cudaGetLastError();
+    switch (G) {
+        case 1: return launch_g<1>(a, bs, ra.opt.grid, s);
+        case 2: return launch_g<2>(a, bs, ra.opt.grid, s);
+        case 4: return launch_g<4>(a, bs, ra.opt.grid, s);
+        case 8: return launch_g<8>(a, bs, ra.opt.grid, s);
+        case 16: return launch_g<16>(a, bs, ra.opt.grid, s);
+        default: return launch_g<32>(a, bs, ra.opt.grid, s);
+    }
 }
 
 }  // namespace eob

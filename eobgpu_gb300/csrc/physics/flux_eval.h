@@ -26,6 +26,7 @@ struct FluxTable {
     double eta;               // clamped symmetric mass ratio used by S_lm
     double equal_mass;        // 1.0 when eta == 0.25 (odd m use f_lm alone)
     double elog[kLMax + 1];   // gamma + log(2 m), m = 1..8: eulerlog_m(v) = elog[m] + log v
+    double gmul[kNumLM];      // m^2 nabs2 / (l!)^2 (lane-group evaluator)
 
     EOB_HD double c_rho(int i, int k) const { return rho[i][k]; }
     EOB_HD double c_rhol(int i, int k) const { return rhol[i][k]; }
@@ -79,6 +80,9 @@ EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *pr
             const int eps = (l + m) % 2;
             const double y = ylm_equator(l - eps, m);
             t->nabs2[i] = (prefix_re[i] * prefix_re[i] + prefix_im[i] * prefix_im[i]) * y * y;
+            double lf = 1.0;
+            for (int j = 2; j <= l; ++j) lf *= (double)j;
+            t->gmul[i] = (double)(m * m) * t->nabs2[i] / (lf * lf);
         }
     t->h22calib = h22calib;
     double eta = nu;
@@ -96,7 +100,7 @@ EOB_HD constexpr double fact2_sq(int l)
 }
 
 struct FluxShared {
-    double v, lv, vphi2, Se, Sodd, x, omega;
+    double v, lv, vphi2, Se, Sodd, x, omega, E1;
 };
 
 // contribution m^2 |h_lm|^2 / (omega^2) of one (l, m); P = prod_{j<=l} (4k^2 + j^2)
@@ -208,5 +212,140 @@ EOB_HD void eob_rhs(const HamCoeffs &h, const Tab &t, const double y[4], double 
     k[2] = -e.dHdr - y[2] / y[3] * fo;
     k[3] = -fo;
 }
+
+EOB_HD void lm_of_index(int i, int *l, int *m)
+{
+    int ll = 2;
+    while (i >= ll) { i -= ll; ++ll; }
+    *l = ll;
+    *m = i + 1;
+}
+
+// one multipole of the flux, l and m at run time: m^2 |h_lm|^2 / omega^2
+template <int KMAX>
+EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, double hw)
+{
+    int l, m;
+    lm_of_index(i, &l, &m);
+    const int eps = (l + m) & 1;
+    const double elm = t.elog[m] + s.lv;
+    double rho = 0.0;
+#pragma unroll
+    for (int k = KMAX; k >= 1; --k) {
+        double ck = t.rho[i][k];
+        if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
+        rho = (rho + ck) * s.v;
+    }
+    rho += 1.0;
+    if (i == 0) {
+        const double v4 = (s.v * s.v) * (s.v * s.v);
+        rho = fma(t.h22calib, v4 * v4 * v4, rho);
+    }
+    // rho^l by squaring (l = 2..8)
+    const double r2 = rho * rho, r4 = r2 * r2;
+    double rpl = (l & 4) ? r4 : 1.0;
+    if (l & 2) rpl *= r2;
+    if (l & 1) rpl *= rho;
+    if (l == 8) rpl = r4 * r4;
+    const double v2 = s.v * s.v;
+    const double aux = s.v * fma(t.f3[i], v2, t.f1[i]);
+    rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
+    const double S = eps ? s.Sodd : s.Se;
+    // vphi^(2 (l + eps)) by squaring
+    const int e = l + eps;
+    const double p2 = s.vphi2 * s.vphi2, p4 = p2 * p2, p8 = p4 * p4;
+    double vpw = (e & 8) ? p8 : 1.0;
+    if (e & 4) vpw *= p4;
+    if (e & 2) vpw *= p2;
+    if (e & 1) vpw *= s.vphi2;
+    // |T_lm|^2 (l!)^2 = (m x)/(1 - e^{-m x}) prod_{j<=l} (4 k^2 + j^2), k = m H omega
+    const double km = m * hw;
+    const double k4 = 4.0 * km * km;
+    double P = 1.0;
+#pragma unroll
+    for (int j = 1; j <= kLMax; ++j) P *= (j <= l) ? (k4 + (double)(j * j)) : 1.0;
+    // e^{-m x} from e^{-x} by squaring (m = 1..8)
+    const double e2 = s.E1 * s.E1, e4 = e2 * e2;
+    double Em = (m & 4) ? e4 : 1.0;
+    if (m & 2) Em *= e2;
+    if (m & 1) Em *= s.E1;
+    if (m == 8) Em = e4 * e4;
+    const double mx = m * s.x;
+    const double T2 = mx / (1.0 - Em) * P;
+    return t.gmul[i] * T2 * (S * S) * (rpl * rpl) * vpw;
+}
+
+
+#ifdef __CUDACC__
+// ---------------------------------------------------------------------------
+// The same flux with the 35 multipoles spread over a group of G lanes that
+// carry the same binary (G = 2 .. 32).  Every lane runs one generic mode
+// evaluation per round, with the mode picked by its position in the group, so
+// the lanes never diverge; modes are ordered by the length of their rho_lm
+// series so that each round's Horner loop is as short as its longest member.
+// The partial sums are combined with butterfly shuffles inside the group.
+
+// slot (lm_index) of the modes ordered by flux rho degree, longest first
+__device__ __constant__ signed char kFluxOrder[kNumLM] = {
+    0, 1,                                  // (2,2) (2,1): degree 10
+    4, 3, 2,                               // (3,3) (3,2) (3,1): 8
+    8, 7, 6, 5, 13,                        // (4,4..1) (5,5): 6
+    11, 9,                                 // (5,3) (5,1): 5
+    12, 10, 19, 17, 15,                    // (5,4) (5,2) (6,6) (6,4) (6,2): 4
+    18, 16, 14, 26, 24, 22, 20,            // (6,5) (6,3) (6,1) (7,7) (7,5) (7,3) (7,1): 3
+    25, 23, 21, 34, 33, 32, 31, 30, 29, 28, 27};  // (7,6) (7,4) (7,2) (8,8..1): 2
+constexpr int kFluxDegSorted[kNumLM] = {10, 10, 8, 8, 8, 6, 6, 6, 6, 6, 5, 5, 4, 4, 4, 4, 4, 3,
+                                        3,  3,  3, 3, 3, 3, 3, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2};
+
+template <int G, int R>
+__device__ __forceinline__ double flux_rounds(const FluxTable &t, const FluxShared &s, double hw, int sub)
+{
+    constexpr int first = R * G;
+    if constexpr (first >= kNumLM) {
+        return 0.0;
+    } else {
+        constexpr int KM = kFluxDegSorted[first];
+        const int pos = first + sub;
+        double here = 0.0;
+        if (pos < kNumLM) here = flux_mode_generic<KM>(t, kFluxOrder[pos], s, hw);
+        return here + flux_rounds<G, R + 1>(t, s, hw, sub);
+    }
+}
+
+template <int G>
+__device__ double flux_eval_group(const FluxTable &t, double r, double pphi, double omega, double Hreal, double omega_c,
+                                  int sub)
+{
+    FluxShared s;
+    s.omega = omega;
+    s.v = cbrt(omega);
+    s.lv = log(s.v);
+    const double vphi_in = 1.0 / (omega_c * omega_c * r * r * r);
+    const double vphi = r * cbrt(vphi_in) * omega;
+    s.vphi2 = vphi * vphi;
+    s.Se = (Hreal * Hreal - 1.0) / (2.0 * t.eta) + 1.0;
+    s.Sodd = s.v * pphi;
+    s.x = 4.0 * kPi * Hreal * omega;
+    s.E1 = exp(-s.x);
+    double part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    return part * omega * omega / (8.0 * kPi);
+}
+
+template <int G>
+__device__ void eob_rhs_group(const HamCoeffs &h, const FluxTable &t, const double y[4], double k[4], int sub)
+{
+    HamEval e;
+    ham_eval(h, y[0], y[2], y[3], &e);
+    const double omega = e.dHdL;
+    const double flux = flux_eval_group<G>(t, y[0], y[3], omega, e.Hreal, e.omega_c, sub) / h.nu;
+    const double fo = flux / omega;
+    k[0] = e.dHdpr;
+    k[1] = omega;
+    k[2] = -e.dHdr - y[2] / y[3] * fo;
+    k[3] = -fo;
+}
+#endif
 
 }  // namespace eob

@@ -114,6 +114,56 @@ class WaveformLikelihood:
         self.last_B = B
         return torch.view_as_complex(out), status
 
+    def prepare(self, params: torch.Tensor, dt: float, order: torch.Tensor | None = None, stages: int = 7,
+                stream=None):
+        """Setup + integrator + multipoles + splines (stages bit mask 1|2|4)."""
+        B = int(params.shape[0])
+        if order is None:
+            order = longest_first(params)
+        rc = self.lib.eob_prepare_stages(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps,
+                                         self.max_modes, self.max_samples, _ptr(params), _ptr(order), B, self.ells,
+                                         self.mms, len(self.modes), float(dt), ctypes.byref(self.options), stages,
+                                         _stream_handle(stream))
+        _lib.check(rc, "eob_prepare_stages")
+        self.last_B = B
+
+    def synth_lnl(self, B: int, data: torch.Tensor, dt: float, amp: float, lnl=None, status=None, stream=None):
+        N = int(data.shape[0])
+        if lnl is None:
+            lnl = torch.empty(B, dtype=torch.float64, device=self.device)
+        if status is None:
+            status = torch.empty(B, dtype=torch.int32, device=self.device)
+        rc = self.lib.eob_synth_lnl(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps, self.max_modes,
+                                    self.max_samples, B, self.mms, len(self.modes), float(dt), _ptr(data), N,
+                                    float(amp), _ptr(lnl), _ptr(status), _stream_handle(stream))
+        _lib.check(rc, "eob_synth_lnl")
+        return lnl, status
+
+    def synth_strain(self, B: int, dt: float, n_samples: int, per_mode: bool = False, status=None, stream=None):
+        K = len(self.modes)
+        shape = (B, K, n_samples, 2) if per_mode else (B, n_samples, 2)
+        out = torch.empty(shape, dtype=torch.float64, device=self.device)
+        if status is None:
+            status = torch.empty(B, dtype=torch.int32, device=self.device)
+        rc = self.lib.eob_synth_strain(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps, self.max_modes,
+                                       self.max_samples, B, self.mms, K, float(dt), int(n_samples), int(per_mode),
+                                       _ptr(out), _ptr(status), _stream_handle(stream))
+        _lib.check(rc, "eob_synth_strain")
+        return torch.view_as_complex(out), status
+
+    def counters(self):
+        """[rows, chunks, rhs_binaries, rhs_all_lanes] of the last run (synchronises)."""
+        buf = (ctypes.c_ulonglong * 8)()
+        _lib.check(self.lib.eob_workspace_counters(_ptr(self.ws), self.max_batch, self.max_steps, self.max_modes,
+                                                   self.max_samples, buf, _stream_handle(None)),
+                   "eob_workspace_counters")
+        return {"rows": int(buf[1]), "chunks": int(buf[2]), "rhs_binaries": int(buf[4]), "rhs_all_lanes": int(buf[5])}
+
+    def npts(self):
+        torch.cuda.synchronize()
+        v = self.views()
+        return self._dev_array(v.npts, self.last_B, torch.int32).cpu().numpy()
+
     # ---- inspection of the last run (tests, API mirror) -----------------
     def views(self) -> _lib.EobViews:
         v = _lib.EobViews()

@@ -46,6 +46,8 @@ typedef struct eob_options {
     int block;              /* integrator threads per block (0 = default) */
     int grid;               /* integrator blocks (0 = one wave of resident blocks) */
     long long max_tries;    /* step attempts per pass before giving up (0 = 2 * max_steps + 100) */
+    int lanes_per_binary;   /* integrator lanes per binary: 1, 2, 4, 8, 16, 32 (0 = chosen from the batch size) */
+    int pad_;
 } eob_options;
 
 void eob_options_default(eob_options *o);
@@ -75,6 +77,11 @@ int eob_waveform_lnl(void *workspace, size_t workspace_bytes, int max_batch, int
 int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
                 const double *params, const int *order, int B, const int *ells, const int *mms, int K, double dt,
                 const eob_options *opt, int *status, cudaStream_t stream);
+/* eob_prepare in parts (for timing each stage): stages bit 1 = setup and
+ * initial conditions, 2 = integrator, 4 = multipoles and splines. */
+int eob_prepare_stages(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
+                       int max_samples, const double *params, const int *order, int B, const int *ells, const int *mms,
+                       int K, double dt, const eob_options *opt, int stages, cudaStream_t stream);
 int eob_synth_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
                   int max_samples, int B, const int *mms, int K, double dt, const double *data, int N, double amp,
                   double *lnl, int *status, cudaStream_t stream);
@@ -112,6 +119,17 @@ typedef struct eob_views {
 } eob_views;
 int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
                         eob_views *out);
+
+/* Host copy of the pipeline's counters after a run (synchronises the stream):
+ * [1] trajectory rows, [2] synthesis chunks, [4] right-hand-side evaluations
+ * spent on binaries, [5] right-hand-side evaluations of all integrator lanes. */
+int eob_workspace_counters(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
+                           unsigned long long *out8, cudaStream_t stream);
+
+/* FP64 issue-rate probe: blocks x threads lanes each run iters x 8 independent
+ * DFMA chains; out[blocks * threads] receives the chain sums.  Timing it gives
+ * the device's FP64 peak used as the integrator's roofline. */
+int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Reference-shaped entry points (src/eob.pyx, src/dopr853.pyx, src/tdinterp.pyx)

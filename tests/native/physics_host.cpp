@@ -45,6 +45,42 @@ void phys_rhs(const double *st, const double *add, int n, double *k)
     }
 }
 
+// flux two ways: specialised per-mode code and the generic lane-group mode evaluator
+void phys_flux_both(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        const double m1 = add[i], m2 = add[n + i], c1 = add[2 * n + i], c2 = add[3 * n + i];
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, m1, m2, c1, c2, 0, 0, 0, 0);
+        const double eta = m1 * m2 / ((m1 + m2) * (m1 + m2));
+        const double chiS = 0.5 * (c1 + c2), chiA = 0.5 * (c1 - c2);
+        const double tpl = (1.0 - 2.0 * eta) * chiS + (m1 - m2) / (m1 + m2) * chiA;
+        static eob::FacCoeffs fc;
+        eob::fac_coeffs_build(&fc, 1, m1, m2, eta, tpl, chiS, chiA);
+        double pre_re[35], pre_im[35];
+        for (int j = 0; j < 35; ++j) { pre_re[j] = add[(10 + 2 * j) * n + i]; pre_im[j] = add[(11 + 2 * j) * n + i]; }
+        static eob::FluxTable t;
+        eob::flux_table_build(&t, fc, pre_re, pre_im, 0.0, h.nu);
+        eob::HamEval e;
+        eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
+        const double omega = e.dHdL;
+        out[2 * i] = eob::flux_eval(t, st[i], st[3 * n + i], omega, e.Hreal, e.omega_c);
+        eob::FluxShared s;
+        s.omega = omega;
+        s.v = cbrt(omega);
+        s.lv = log(s.v);
+        const double vphi = st[i] * cbrt(1.0 / (e.omega_c * e.omega_c * st[i] * st[i] * st[i])) * omega;
+        s.vphi2 = vphi * vphi;
+        s.Se = (e.Hreal * e.Hreal - 1.0) / (2.0 * t.eta) + 1.0;
+        s.Sodd = s.v * st[3 * n + i];
+        s.x = 4.0 * eob::kPi * e.Hreal * omega;
+        s.E1 = exp(-s.x);
+        double sum = 0.0;
+        for (int j = 0; j < 35; ++j) sum += eob::flux_mode_generic<10>(t, j, s, e.Hreal * omega);
+        out[2 * i + 1] = sum * omega * omega / (8.0 * eob::kPi);
+    }
+}
+
 // Newtonian prefixes of one binary, interleaved (re, im) x 35
 void phys_prefixes(double m1, double m2, double *out)
 {

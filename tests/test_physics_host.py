@@ -1,0 +1,76 @@
+"""The product's device physics (eobgpu_gb300/csrc/physics/*.h) compiled for
+the host and checked against the reference's golden outputs: Hamiltonian and
+gradient (u-jet evaluation), RHS (table-driven flux), the generic multipole
+evaluator used by lane groups, and the Newtonian prefixes."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def phys(tmp_path_factory):
+    out = tmp_path_factory.mktemp("phys") / "libphys.so"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", str(out),
+                           os.path.join(HERE, "native", "physics_host.cpp")])
+    return ctypes.CDLL(str(out))
+
+
+P = ctypes.POINTER(ctypes.c_double)
+
+
+def dp(a):
+    return a.ctypes.data_as(P)
+
+
+def test_ham_eval_vs_reference(phys, golden):
+    g = golden["ham_rhs"]
+    st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
+    n = st.shape[1]
+    out = np.zeros(5 * n)
+    phys.phys_ham(dp(st), dp(add), ctypes.c_int(n), dp(out))
+    out = out.reshape(n, 5).T
+    ok = np.isfinite(g["H"])
+    assert np.max(np.abs(out[0][ok] / g["H"][ok] - 1)) < 1e-13
+    gr = g["grad"]
+    sc = np.abs(gr[:, ok]).max(axis=0)
+    for j, q in ((1, 0), (2, 2), (3, 3)):
+        assert np.max(np.abs(out[j][ok] - gr[q][ok]) / sc) < 1e-12
+
+
+def test_rhs_vs_reference(phys, golden):
+    g = golden["ham_rhs"]
+    st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
+    n = st.shape[1]
+    k = np.zeros(4 * n)
+    phys.phys_rhs(dp(st), dp(add), ctypes.c_int(n), dp(k))
+    k = k.reshape(4, n)
+    ref = g["rhs"]
+    ok = np.all(np.isfinite(ref), axis=0)
+    np.testing.assert_array_equal(np.all(np.isfinite(k), axis=0), ok)
+    assert np.max(np.abs(k[:, ok] - ref[:, ok]) / np.abs(ref[:, ok]).max(axis=0)) < 1e-12
+
+
+def test_generic_flux_matches_specialised(phys, golden):
+    g = golden["ham_rhs"]
+    st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
+    n = st.shape[1]
+    out = np.zeros(2 * n)
+    phys.phys_flux_both(dp(st), dp(add), ctypes.c_int(n), dp(out))
+    out = out.reshape(n, 2)
+    ok = np.isfinite(out[:, 0])
+    assert ok.sum() > 0.9 * n
+    assert np.max(np.abs(out[ok, 1] / out[ok, 0] - 1)) < 1e-13
+
+
+def test_newton_prefixes(phys):
+    from golden.make_golden import newton_prefixes
+    for m1, m2 in ((0.6, 0.4), (0.5, 0.5), (0.9, 0.1)):
+        pre = np.zeros(70)
+        phys.phys_prefixes(ctypes.c_double(m1), ctypes.c_double(m2), dp(pre))
+        ref = newton_prefixes(m1, m2)
+        assert np.max(np.abs(pre[0::2] + 1j * pre[1::2] - ref)) < 1e-14 * np.abs(ref).max()
