@@ -216,7 +216,8 @@ def config_block(cfg, args, extra=None):
          "total_mass_msun": list(cfg.total_mass), "mass_ratio": list(cfg.mass_ratio), "chi": list(cfg.chi),
          "f0_hz": list(cfg.f0), "modes": [list(m) for m in cfg.modes], "dt_s": cfg.dt, "n_samples": cfg.n_samples,
          "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12, "queue": "longest first",
-         "l2": "flushed between timed steps (256 MiB write)"}
+         "l2": "flushed between timed steps (256 MiB write)",
+         "lanes_per_binary": getattr(args, "lanes", 0) or "auto"}
     if extra:
         d.update(extra)
     return d
@@ -249,6 +250,7 @@ def main():
     ap.add_argument("--max-steps", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0, help="integrator lanes per binary (0: chosen from the batch size)")
     ap.add_argument("--census", action="store_true",
                     help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
     args = ap.parse_args()
@@ -282,7 +284,10 @@ def main():
     params, data, amp = make_inputs(cfg, rank, device, args.max_steps)
     B = params.shape[0]
     K = len(cfg.modes)
-    wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device)
+    from eobgpu_gb300 import _lib
+    opt = _lib.default_options()
+    opt.lanes_per_binary = args.lanes
+    wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device, options=opt)
     P = torch.tensor(params, device=device)
     D = torch.tensor(data, device=device)
     order = longest_first(P)

@@ -33,13 +33,13 @@ struct WsLayout {
     int Bc, Lc, Kc, Nc, nsubs, max_chunks;
 };
 
-EOB_HD size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+EOB_HD constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Offsets of every array inside the workspace for capacities (Bc binaries,
 // Lc trajectory rows per binary, Kc modes, Nc samples).
-EOB_HD WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
+EOB_HD constexpr WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
 {
-    WsLayout w;
+    WsLayout w{};
     w.Bc = Bc; w.Lc = Lc; w.Kc = Kc; w.Nc = Nc;
     w.nsubs = 1 + 2 * Kc;
     w.max_chunks = Bc * ((Nc + kChunk - 1) / kChunk);

@@ -74,6 +74,15 @@ class WaveformLikelihood:
         self.mms = (ctypes.c_int * 5)(*[m for _, m in self.modes])
         self.last_B = 0
 
+    def set_modes(self, modes):
+        """Modes of the following calls (at most max_modes of them)."""
+        modes = [tuple(int(v) for v in m) for m in modes]
+        if not 1 <= len(modes) <= self.max_modes:
+            raise _lib.EOBError(f"{len(modes)} modes for a workspace of {self.max_modes}")
+        self.modes = modes
+        self.ells = (ctypes.c_int * 5)(*[l for l, _ in modes])
+        self.mms = (ctypes.c_int * 5)(*[m for _, m in modes])
+
     def run(self, params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, order: torch.Tensor | None = None,
             lnl: torch.Tensor | None = None, status: torch.Tensor | None = None, stream=None):
         """lnL for every binary of params[B, 5] (m1, m2 [Msun], chi1, chi2, f0 [Hz])."""

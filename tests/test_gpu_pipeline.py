@@ -52,8 +52,11 @@ def test_config1_trajectory_rows(cfg1_run):
     for b, (t, y) in enumerate(trajs):
         L = nsteps[b]
         assert t[0] == 0.0 and np.all(np.diff(t) > 0)
-        # fixed 0.05 M steps at the end of the fine pass
-        np.testing.assert_allclose(np.diff(t[-20:]), 0.05, rtol=1e-12)
+        # the fine pass takes fixed steps of 0.05 M, halved after each rejection
+        d = np.diff(t[-20:])
+        assert np.all(d <= 0.05 + 1e-9)
+        ratio = 0.05 / d
+        assert np.allclose(ratio, 2.0 ** np.round(np.log2(ratio)), rtol=1e-6)
         assert abs(t[-1] - c["traj_t"][b, L - 1]) < 0.05
 
 
@@ -86,3 +89,22 @@ def test_config1_lnl_vs_oracle(cfg1_run, oracle):
     for b in range(len(lnl)):
         r = oracle.lnl_one(c["params"][b], float(c["dt"]), int(c["N"]), [(2, 2)], c["data"], float(c["amp"]))
         assert abs(lnl[b] / r["lnl"] - 1) < 1e-9, (b, lnl[b], r["lnl"])
+
+
+@pytest.mark.parametrize("G", [1, 2, 4, 8, 16, 32])
+def test_config1_lanes_per_binary(torch_cuda, golden, G):
+    """Every lanes-per-binary variant of the integrator gives the reference's lnL."""
+    torch = torch_cuda
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    c = golden["config1"]
+    opt = _lib.default_options()
+    opt.lanes_per_binary = G
+    wl = WaveformLikelihood(max_batch=8, max_steps=4096, modes=[(2, 2)], max_samples=int(c["N"]), options=opt)
+    lnl, st = wl.run(torch.tensor(c["params"], device="cuda"), torch.tensor(c["data"], device="cuda"),
+                     float(c["dt"]), float(c["amp"]))
+    lnl = lnl.cpu().numpy()
+    assert np.all(st.cpu().numpy() == 0)
+    assert np.all(np.abs(lnl / c["lnl"] - 1) < 1e-9), (G, lnl / c["lnl"] - 1)
+    nsteps, npts, _, _ = wl.trajectories()
+    np.testing.assert_array_equal(nsteps, c["nsteps"])
