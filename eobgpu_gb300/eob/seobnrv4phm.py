@@ -8,7 +8,7 @@ loop; the step-by-step methods (setup_class, get_initial_conditions,
 run_trajectory, get_hlms) are kept on the reference-shaped entry points for
 callers that use them directly.
 
-Differences from the reference, all deliberate and documented in the design doc:
+Differences from the reference, all deliberate:
 * max_step defaults to 20000 trajectory rows (the reference hard-codes 400,
   eob/seobnrv4phm.py:1899, which long binaries exceed);
 * each binary's result is what the reference returns for that binary alone
