@@ -50,6 +50,9 @@ _SIGS = {
                                  _P, _P, _P]),
     "eob_workspace_counters": (c_int, [_P, c_int, c_int, c_int, c_int, _P, _P]),
     "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
+    "eob_noalloc_scratch_bytes": (c_size_t, []),
+    "eob_waveform_lnl_noalloc": (c_int, [_P, c_int, _P, _P, c_int, c_double, _P, c_int, c_double,
+                                         ctypes.POINTER(EobOptions), _P, _P, _P]),
     "eob_workspace_views": (c_int, [_P, c_int, c_int, c_int, c_int, ctypes.POINTER(EobViews)]),
     "eob_evaluate_ham": (c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, c_double, c_double, c_double, c_double, c_int,
                                  _P]),

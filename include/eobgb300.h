@@ -92,6 +92,25 @@ int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int
                      int max_samples, int B, const int *mms, int K, double dt, int N, int per_mode, double *out,
                      int *status, cudaStream_t stream);
 
+/* eob_waveform_lnl for callers that cannot allocate device memory (no
+ * counterpart in the reference).  Code that runs inside another framework's
+ * memory pool, a plugin host without allocator access, or a process that must
+ * not call cudaMalloc while other work is in flight passes only its inputs
+ * and outputs; the scratch is a fixed __device__ array of
+ * eob_noalloc_scratch_bytes() bytes (about 12 MB) that every GPU loading the
+ * library keeps until exit.  Limits: B <= 16 binaries, K = 1 mode,
+ * N <= 8192 samples, at most 4096 trajectory rows per binary (longer
+ * trajectories end with EOB_ST_MAXSTEP); larger calls return EOB_E_ARG.
+ * The first call on a device looks up the array's address and should come
+ * before any stream capture.  All calls share the array and it keeps the
+ * last call's contents: calls that overlap on the GPU (other streams or
+ * threads) race and must be serialised by the caller.  Allocates nothing
+ * (no cudaMalloc, cudaFree or allocating library call). */
+size_t eob_noalloc_scratch_bytes(void);
+int eob_waveform_lnl_noalloc(const double *params, int B, const int *ells, const int *mms, int K, double dt,
+                             const double *data, int N, double amp, const eob_options *opt, double *lnl, int *status,
+                             cudaStream_t stream);
+
 /* Same pipeline, writing the summed strain instead of the likelihood:
  * strain[B][N] complex (re, im interleaved) = sum_lm h_lm(t_k) on the grid
  * t_k = k dt from each binary's start, zero past its last sample (the
