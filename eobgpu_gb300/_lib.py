@@ -25,7 +25,7 @@ class EobOptions(ctypes.Structure):
 
 
 class EobViews(ctypes.Structure):
-    _fields_ = [("traj", c_void_p), ("nsteps", c_void_p), ("status", c_void_p), ("npts", c_void_p),
+    _fields_ = [("bins", c_void_p), ("traj", c_void_p), ("nsteps", c_void_p), ("status", c_void_p), ("npts", c_void_p),
                 ("row_off", c_void_p), ("tin", c_void_p), ("spline_y", c_void_p), ("spline_c1", c_void_p),
                 ("spline_c2", c_void_p), ("spline_c3", c_void_p), ("row_capacity", c_int),
                 ("rows_capacity", c_ll), ("nsubs", c_int)]
@@ -45,11 +45,12 @@ _SIGS = {
     "eob_prepare_stages": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, _P, _P, c_int, _P, _P, c_int,
                                    c_double, ctypes.POINTER(EobOptions), c_int, _P]),
     "eob_synth_lnl": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, c_int, _P, c_int, c_double, _P, c_int,
-                              c_double, _P, _P, _P]),
+                              c_double, ctypes.POINTER(EobOptions), _P, _P, _P]),
     "eob_synth_strain": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, c_int, _P, c_int, c_double, c_int, c_int,
                                  _P, _P, _P]),
     "eob_workspace_counters": (c_int, [_P, c_int, c_int, c_int, c_int, _P, _P]),
     "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
+    "eob_component_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
     "eob_noalloc_scratch_bytes": (c_size_t, []),
     "eob_waveform_lnl_noalloc": (c_int, [_P, c_int, _P, _P, c_int, c_double, _P, c_int, c_double,
                                          ctypes.POINTER(EobOptions), _P, _P, _P]),

@@ -81,7 +81,7 @@ int eob_prepare(void *workspace, size_t workspace_bytes, int max_batch, int max_
 
 static int synth(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples,
                  int B, const int *mms, int K, double dt, const double *data, int N, double amp, double *lnl,
-                 int mode, double *out, int *status, cudaStream_t stream)
+                 int mode, double *out, int *status, const eob_options *opt, cudaStream_t stream)
 {
     WsLayout L;
     if (!workspace || !dims_ok(workspace_bytes, max_batch, max_steps, max_modes, max_samples, &L)) return EOB_E_ARG;
@@ -98,6 +98,7 @@ static int synth(void *workspace, size_t workspace_bytes, int max_batch, int max
     a.amp = amp;
     a.lnl = lnl;
     a.status_out = status;
+    if (opt) a.opt = *opt; else eob_options_default(&a.opt);
     const Ws w = ws_views(workspace, L);
     const cudaError_t e = launch_synth(w, a, mode, out, stream);
     return e == cudaSuccess ? EOB_OK : EOB_E_CUDA;
@@ -105,11 +106,11 @@ static int synth(void *workspace, size_t workspace_bytes, int max_batch, int max
 
 int eob_synth_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
                   int max_samples, int B, const int *mms, int K, double dt, const double *data, int N, double amp,
-                  double *lnl, int *status, cudaStream_t stream)
+                  const eob_options *opt, double *lnl, int *status, cudaStream_t stream)
 {
     if (!data || !lnl) return EOB_E_ARG;
     return synth(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, data, N, amp,
-                 lnl, 0, nullptr, status, stream);
+                 lnl, 0, nullptr, status, opt, stream);
 }
 
 int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
@@ -118,7 +119,7 @@ int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int
 {
     if (!out) return EOB_E_ARG;
     return synth(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, nullptr, N,
-                 1.0, nullptr, per_mode ? 2 : 1, out, status, stream);
+                 1.0, nullptr, per_mode ? 2 : 1, out, status, nullptr, stream);
 }
 
 int eob_waveform_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
@@ -131,7 +132,7 @@ int eob_waveform_lnl(void *workspace, size_t workspace_bytes, int max_batch, int
                          ells, mms, K, dt, opt, nullptr, stream);
     if (rc != EOB_OK) return rc;
     return eob_synth_lnl(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, data,
-                         N, amp, lnl, status, stream);
+                         N, amp, opt, lnl, status, stream);
 }
 
 int eob_waveform_strain(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
@@ -143,8 +144,8 @@ int eob_waveform_strain(void *workspace, size_t workspace_bytes, int max_batch, 
     int rc = eob_prepare(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, params, order, B,
                          ells, mms, K, dt, opt, nullptr, stream);
     if (rc != EOB_OK) return rc;
-    return eob_synth_strain(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, N,
-                            0, strain, status, stream);
+    return synth(workspace, workspace_bytes, max_batch, max_steps, max_modes, max_samples, B, mms, K, dt, nullptr, N,
+                 1.0, nullptr, 1, strain, status, opt, stream);
 }
 
 int eob_workspace_counters(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
@@ -165,6 +166,7 @@ int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_m
     const WsLayout L = ws_layout(max_batch, max_steps, max_modes, max_samples);
     if (L.total == 0) return EOB_E_ARG;
     const Ws w = ws_views(workspace, L);
+    out->bins = w.bins;
     out->traj = w.traj;
     out->nsteps = w.nsteps;
     out->status = w.status;

@@ -29,7 +29,8 @@ constexpr int kChunk = 1024;   // samples per synthesis work item
 constexpr int kTrajStride = 5; // t, r, phi, pr, pphi per trajectory row
 
 struct WsLayout {
-    size_t bins, fac, traj, nsteps, status, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, total;
+    size_t bins, fac, traj, nsteps, status, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, f32,
+        dataf, total;
     int Bc, Lc, Kc, Nc, nsubs, max_chunks;
 };
 
@@ -61,6 +62,8 @@ EOB_HD constexpr WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
     w.cC = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
     w.cD = o;        o = align256(o + sizeof(double) * rows * w.nsubs);
     w.partial = o;   o = align256(o + sizeof(double) * (size_t)w.max_chunks);
+    w.f32 = o;       o = align256(o + sizeof(float) * 4 * rows * 2 * (size_t)Kc);
+    w.dataf = o;     o = align256(o + sizeof(float) * (size_t)Nc);
     w.total = o;
     return w;
 }
@@ -72,10 +75,13 @@ struct Ws {
     double *traj;
     int *nsteps, *status;
     unsigned long long *queue;  // [0] work queue, [1] total rows, [2] total chunks, [3] sum data^2 (double bits),
-                                // [4] RHS evaluations for binaries, [5] RHS evaluations incl. idle lanes
+                                // [4] RHS evaluations for binaries, [5] RHS evaluations incl. idle lanes,
+                                // [6] 1 if the spline build wrote FP32 copies (mixed precision)
     long long *row_off, *chunk_off;
     int *npts;
     double *tin, *ys, *cA, *cB, *cC, *cD, *partial;
+    float *f32;    // mixed precision: y, c1, c2, c3 of the mode series, [4][2K][rows]
+    float *dataf;  // mixed precision: data in FP32
     WsLayout L;
 };
 
@@ -99,6 +105,8 @@ inline Ws ws_views(void *base, const WsLayout &L)
     w.cC = (double *)(b + L.cC);
     w.cD = (double *)(b + L.cD);
     w.partial = (double *)(b + L.partial);
+    w.f32 = (float *)(b + L.f32);
+    w.dataf = (float *)(b + L.dataf);
     w.L = L;
     return w;
 }
@@ -122,7 +130,8 @@ struct RunArgs {
 cudaError_t launch_setup(const Ws &w, const RunArgs &a, cudaStream_t s);
 cudaError_t launch_integrate(const Ws &w, const RunArgs &a, cudaStream_t s);
 cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s);
-// mode 0: lnL (a.data, a.lnl); 1: summed strain out[B][N]; 2: per-mode out[B][K][N], t clamped to each end
+// mode 0: lnL (a.data, a.lnl; a.opt.precision 1 = mixed); 1: summed strain out[B][N];
+// 2: per-mode out[B][K][N], t clamped to each end
 cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, cudaStream_t s);
 
 }  // namespace eob

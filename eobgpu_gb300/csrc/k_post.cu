@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_rows(Ws w, int B, double 
 
 // synthesis work items: chunks of kChunk samples of min(npts, N) samples per
 // binary (all N samples when cover_all); sum of data^2
-__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Ws w, int B, int N, int cover_all, const double *data)
+__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Ws w, int B, int N, int cover_all, const double *data,
+                                                               int mixed)
 {
     __shared__ long long sm[kScanThreads];
     __shared__ double s_sq[kScanThreads];
@@ -108,7 +109,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Ws w, int B, int N
     }
     double sq = 0.0;
     if (data)
-        for (int k = tid; k < N; k += kScanThreads) sq += data[k] * data[k];
+        for (int k = tid; k < N; k += kScanThreads) {
+            sq += data[k] * data[k];
+            if (mixed) w.dataf[k] = (float)data[k];
+        }
     s_sq[tid] = sq;
     long long total;
     long long co = block_exclusive_scan<kScanThreads>(chunks, sm, &total);
@@ -214,10 +218,11 @@ __device__ void spline_one(const double *x, const double *y, int n, double *Bv, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_spline(Ws w, int B, int nsubs)
+__global__ void __launch_bounds__(128) k_spline(Ws w, int B, int nsubs, int mixed)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= B * nsubs) return;
+    if (idx == 0) w.queue[6] = (unsigned long long)mixed;
     const int b = idx / nsubs, sub = idx % nsubs;
     if (w.npts[b] <= 0) return;
     const int n = w.nsteps[b];
@@ -225,6 +230,17 @@ __global__ void __launch_bounds__(128) k_spline(Ws w, int B, int nsubs)
     const size_t base = (size_t)w.row_off[b];
     const size_t o = (size_t)sub * Rc + base;
     spline_one(w.tin + base, w.ys + o, n, w.cD + o, w.cA + o, w.cB + o, w.cC + o);
+    if (mixed && sub >= 1) {
+        // FP32 copies of the amplitude series for the mixed-precision synthesis
+        const size_t S = (size_t)2 * w.L.Kc * Rc;
+        float *f = w.f32 + (size_t)(sub - 1) * Rc + base;
+        for (int i = 0; i < n; ++i) {
+            f[i] = (float)w.ys[o + i];
+            f[S + i] = (float)w.cA[o + i];
+            f[2 * S + i] = (float)w.cB[o + i];
+            f[3 * S + i] = (float)w.cC[o + i];
+        }
+    }
 }
 
 struct SynthArgs {
@@ -316,6 +332,83 @@ __global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
     }
 }
 
+// Mixed precision synthesis: the phase spline and its reduction mod 2 pi run
+// in FP64; the amplitude splines (FP32 coefficient copies written at spline
+// build), sin/cos and the residual run in FP32.  mode 0 accumulates the lnL
+// terms with a Kahan-compensated FP32 sum per thread and FP64 chunk partials;
+// mode 1 writes the summed strain (zero past each waveform's end).  The
+// FP32 copies exist only if the spline build ran with precision 1 (workspace
+// flag queue[6]); otherwise the lnL comes out NaN.
+__global__ void __launch_bounds__(256) k_synth_mixed(Ws w, SynthArgs sa)
+{
+    __shared__ double s_red[256 / 32];
+    const long long C = (long long)w.queue[2];
+    const bool have_f32 = w.queue[6] == 1ull;
+    const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
+    const size_t S = (size_t)2 * w.L.Kc * Rc;
+    const double two_pi_hi = 6.283185307179586232, two_pi_lo = 2.4492935982947064e-16;
+    for (long long c = blockIdx.x; c < C; c += gridDim.x) {
+        const int b = find_segment(w.chunk_off, sa.B, c);
+        const int j = (int)(c - w.chunk_off[b]);
+        const int np = w.npts[b];
+        const int nuse = np < sa.N ? np : sa.N;
+        const int n = w.nsteps[b];
+        const size_t base = (size_t)w.row_off[b];
+        const double *x = w.tin + base;
+        const double Mts = w.bins[b].Mt * kMTSUN_SI;
+        const double dT = sa.dt / Mts;
+        const double t0 = x[0], tend = x[n - 1];
+        float acc = 0.0f, comp = 0.0f;
+        const int kbeg = j * kChunk;
+        const int kend = have_f32 ? min(nuse, kbeg + kChunk) : kbeg;
+        for (int k = kbeg + threadIdx.x; k < kend; k += blockDim.x) {
+            double t = k * dT + t0;
+            if (t > tend) t = tend;
+            const int i = knot_index(x, n, t);
+            const double xx = t - x[i];
+            const size_t o = base + i;
+            const double phi = w.ys[o] + xx * (w.cA[o] + xx * (w.cB[o] + xx * w.cC[o]));
+            const float xf = (float)xx;
+            float h = 0.0f, hi = 0.0f;
+            for (int q = 0; q < sa.K; ++q) {
+                const size_t orr = (size_t)(2 * q) * Rc + o, oi = (size_t)(2 * q + 1) * Rc + o;
+                const float re = w.f32[orr] + xf * (w.f32[S + orr] + xf * (w.f32[2 * S + orr] + xf * w.f32[3 * S + orr]));
+                const float im = w.f32[oi] + xf * (w.f32[S + oi] + xf * (w.f32[2 * S + oi] + xf * w.f32[3 * S + oi]));
+                const double ph = sa.mms[q] * phi;
+                const double nn = rint(ph * 0.15915494309189533577);
+                const double red = fma(-nn, two_pi_lo, fma(-nn, two_pi_hi, ph));
+                float sp, cp;
+                sincosf((float)red, &sp, &cp);
+                // (re + i im) e^{-i m phi}
+                h = fmaf(re, cp, fmaf(im, sp, h));
+                hi = fmaf(im, cp, fmaf(-re, sp, hi));
+            }
+            if (sa.mode == 1) {
+                sa.out[2 * ((size_t)b * sa.N + k)] = (double)h;
+                sa.out[2 * ((size_t)b * sa.N + k) + 1] = (double)hi;
+            } else {
+                const float hk = (float)sa.amp * h;
+                const float term = hk * (hk - 2.0f * w.dataf[k]);
+                // Kahan summation
+                const float yv = term - comp;
+                const float tv = acc + yv;
+                comp = (tv - acc) - yv;
+                acc = tv;
+            }
+        }
+        double dacc = (double)acc - (double)comp;
+        for (int off = 16; off > 0; off >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, off);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = dacc;
+        __syncthreads();
+        if (threadIdx.x == 0 && sa.mode == 0) {
+            double sum = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += s_red[q];
+            w.partial[c] = have_f32 ? sum : __longlong_as_double(0x7ff8000000000000ll);
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_finalize(Ws w, int B, double *lnl, int *status_out)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,7 +433,7 @@ cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s)
     for (int j = 0; j < kMaxModes; ++j) { ma.ells[j] = a.ells[j]; ma.mms[j] = a.mms[j]; }
     k_modes<<<nsm * 8, 128, 0, s>>>(w, a.B, ma);
     const int nsubs = 1 + 2 * a.K;
-    k_spline<<<(a.B * nsubs + 127) / 128, 128, 0, s>>>(w, a.B, nsubs);
+    k_spline<<<(a.B * nsubs + 127) / 128, 128, 0, s>>>(w, a.B, nsubs, a.opt.precision == 1 ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -349,7 +442,9 @@ cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, c
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    k_scan_chunks<<<1, kScanThreads, 0, s>>>(w, a.B, a.N, mode == 2 ? 1 : 0, mode == 0 ? a.data : nullptr);
+    const int mixed = (mode != 2 && a.opt.precision == 1) ? 1 : 0;
+    k_scan_chunks<<<1, kScanThreads, 0, s>>>(w, a.B, a.N, mode == 2 ? 1 : 0, mode == 0 ? a.data : nullptr,
+                                             mode == 0 ? mixed : 0);
     if (mode == 1) {
         cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * 2 * (size_t)a.B * a.N, s);
         if (e != cudaSuccess) return e;
@@ -364,7 +459,8 @@ cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, c
     sa.data = a.data;
     sa.out = out;
     sa.mode = mode;
-    k_synth<<<nsm * 8, 256, 0, s>>>(w, sa);
+    if (mixed) k_synth_mixed<<<nsm * 8, 256, 0, s>>>(w, sa);
+    else k_synth<<<nsm * 8, 256, 0, s>>>(w, sa);
     k_finalize<<<(a.B + 127) / 128, 128, 0, s>>>(w, a.B, mode == 0 ? a.lnl : nullptr, a.status_out);
     return cudaGetLastError();
 }

@@ -15,6 +15,60 @@ __global__ void k_fp64_probe(double *out, int iters)
 }
 }  // namespace
 
+// Component timing: every thread evaluates one piece of the right-hand side
+// `iters` times on binary 0 of a prepared workspace (states varied slightly
+// so nothing is hoisted).  With one warp per SM sub-partition the FP64 pipe
+// sets the pace, so time / iters / 64 cycles = FP64 instructions per call.
+template <int WHICH>
+__global__ void k_component(const eob::BinaryRec *bins, int iters, double *out)
+{
+    const eob::BinaryRec &b = bins[0];
+    const int lane = threadIdx.x & 31;
+    double r = 12.0 + 1e-3 * threadIdx.x, pr = -1e-3, L = 3.9, acc = 0.0;
+    for (int i = 0; i < iters; ++i) {
+        r += 1e-9;
+        if (WHICH == 0) {
+            eob::HamEval e;
+            eob::ham_eval(b.ham, r, pr, L, &e);
+            acc += e.dHdr + e.dHdpr + e.dHdL + e.omega_c + e.Hreal;
+        } else if (WHICH == 1) {
+            acc += eob::flux_eval(b.flux, r, L, 0.0227 + 1e-12 * i, 0.987, 0.0226);
+        } else if (WHICH == 2) {
+            const double y[4] = {r, 0.0, pr, L};
+            double k[4];
+            eob::eob_rhs(b.ham, b.flux, y, k);
+            acc += k[0] + k[1] + k[2] + k[3];
+        } else if (WHICH == 3) {
+            const double y[4] = {r, 0.0, pr, L};
+            double k[4];
+            eob::eob_rhs_group<16>(b.ham, b.flux, y, k, lane & 15);
+            acc += k[0] + k[1] + k[2] + k[3];
+        } else if (WHICH == 4) {
+            acc += eob::flux_eval_group<16>(b.flux, r, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane & 15);
+        } else if (WHICH == 5) {
+            acc += eob::flux_eval_group<32>(b.flux, r, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane);
+        }
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+extern "C" int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
+                                   cudaStream_t stream)
+{
+    if (!bins || !out || blocks < 1 || threads < 32 || threads > 1024 || iters < 1) return EOB_E_ARG;
+    const eob::BinaryRec *b = (const eob::BinaryRec *)bins;
+    switch (which) {
+        case 0: k_component<0><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 1: k_component<1><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 2: k_component<2><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 3: k_component<3><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 4: k_component<4><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 5: k_component<5><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        default: return EOB_E_ARG;
+    }
+    return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
+}
+
 extern "C" int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream)
 {
     if (!out || blocks < 1 || threads < 1 || threads > 1024 || iters < 1) return EOB_E_ARG;

@@ -144,7 +144,8 @@ class WaveformLikelihood:
             status = torch.empty(B, dtype=torch.int32, device=self.device)
         rc = self.lib.eob_synth_lnl(_ptr(self.ws), self.ws_bytes, self.max_batch, self.max_steps, self.max_modes,
                                     self.max_samples, B, self.mms, len(self.modes), float(dt), _ptr(data), N,
-                                    float(amp), _ptr(lnl), _ptr(status), _stream_handle(stream))
+                                    float(amp), ctypes.byref(self.options), _ptr(lnl), _ptr(status),
+                                    _stream_handle(stream))
         _lib.check(rc, "eob_synth_lnl")
         return lnl, status
 

@@ -42,7 +42,9 @@ typedef struct eob_options {
     double step_back;       /* restart offset [M]; reference 10 (eob/seobnrv4phm.py:2072) */
     double fine_step;       /* fixed fine step [M]; reference 0.05 */
     int ic_mode;            /* 0: reference-effective p_r0, 1: physical (exact Hessian) */
-    int precision;          /* 0: FP64 synthesis + lnL, 1: mixed (FP32 amplitude/sincos, compensated sum) */
+    int precision;          /* 0: FP64 synthesis + lnL; 1: mixed -- phase in FP64 and reduced mod 2 pi, amplitude
+                               splines, sin/cos and the residual in FP32 with compensated sums (pass the same value
+                               to the prepare and synth calls) */
     int block;              /* integrator threads per block (0 = default) */
     int grid;               /* integrator blocks (0 = one wave of resident blocks) */
     long long max_tries;    /* step attempts per pass before giving up (0 = 2 * max_steps + 100) */
@@ -84,7 +86,7 @@ int eob_prepare_stages(void *workspace, size_t workspace_bytes, int max_batch, i
                        int K, double dt, const eob_options *opt, int stages, cudaStream_t stream);
 int eob_synth_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
                   int max_samples, int B, const int *mms, int K, double dt, const double *data, int N, double amp,
-                  double *lnl, int *status, cudaStream_t stream);
+                  const eob_options *opt, double *lnl, int *status, cudaStream_t stream);
 /* per_mode = 0: out[B][N] complex = sum_lm h_lm(t_k), zero past each binary's last sample;
  * per_mode = 1: out[B][K][N] complex per mode with t_k clamped to each binary's last sample
  * (the uniform-grid modes of SEOBNRv4PHM.__call__, eob/seobnrv4phm.py:2336-2372). */
@@ -124,6 +126,7 @@ int eob_waveform_strain(void *workspace, size_t workspace_bytes, int max_batch, 
  * traj[b][row][5] = (t [M], r, phi, pr, pphi), nsteps[b] rows each;
  * npts[b] uniform-grid samples of each binary's waveform. */
 typedef struct eob_views {
+    void *bins;           /* per-binary coefficient records */
     double *traj;
     int *nsteps;
     int *status;
@@ -149,6 +152,12 @@ int eob_workspace_counters(void *workspace, int max_batch, int max_steps, int ma
  * DFMA chains; out[blocks * threads] receives the chain sums.  Timing it gives
  * the device's FP64 peak used as the integrator's roofline. */
 int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream);
+/* Timing probe of one piece of the right-hand side on binary 0 of a prepared
+ * workspace (bins from eob_workspace_views): which = 0 Hamiltonian and
+ * gradient, 1 flux, 2 right-hand side, 3 right-hand side with 16 lanes per
+ * binary, 4 flux with 16 lanes, 5 flux with 32 lanes. */
+int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
+                        cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Reference-shaped entry points (src/eob.pyx, src/dopr853.pyx, src/tdinterp.pyx)

@@ -1,0 +1,96 @@
+"""The C-ABI library on the host (no GPU): it loads, exports every function
+include/eobgb300.h declares, the ctypes mirror matches the C struct layouts,
+and the host-only entry points (defaults, workspace sizing) behave."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from eobgpu_gb300 import _lib
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+HEADER = os.path.join(ROOT, "include", "eobgb300.h")
+
+
+def _declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^(?:int|size_t|void)\s+\**(eob_[a-z0-9_]+)\(", txt, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("native library not built")
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib._SIGS, f"{n} has no ctypes signature"
+
+
+def test_struct_layouts_match_header(lib):
+    src = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "eobgb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu\n", sizeof(eob_options), offsetof(eob_options, ic_mode),
+         offsetof(eob_options, max_tries), offsetof(eob_options, lanes_per_binary), sizeof(eob_views));
+  printf("%zu %zu %zu\n", offsetof(eob_views, row_capacity), offsetof(eob_views, rows_capacity),
+         offsetof(eob_views, nsubs));
+  return 0;
+}
+"""
+    cuda_inc = "/usr/local/cuda/include"
+    if not os.path.isdir(cuda_inc):
+        pytest.skip("CUDA headers not found")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "l.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "l")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, c, "-o", exe], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    o, v = _lib.EobOptions, _lib.EobViews
+    want = [ctypes.sizeof(o), o.ic_mode.offset, o.max_tries.offset, o.lanes_per_binary.offset, ctypes.sizeof(v),
+            v.row_capacity.offset, v.rows_capacity.offset, v.nsubs.offset]
+    assert [int(x) for x in out] == want
+
+
+def test_default_options(lib):
+    o = _lib.default_options()
+    # the reference's controller and two-pass constants
+    assert o.rtol == 1e-12 and o.atol == 1e-12
+    assert o.h_init == 0.01 and o.step_back == 10.0 and o.fine_step == 0.05
+    assert o.ic_mode == 0 and o.precision == 0
+
+
+def test_workspace_sizing(lib):
+    f = lib.eob_workspace_bytes
+    a = f(8, 4000, 1, 8192)
+    assert a > 0 and a % 256 == 0
+    assert f(16, 4000, 1, 8192) > a
+    assert f(8, 8000, 1, 8192) > a
+    assert f(8, 4000, 5, 8192) > a
+    assert f(8, 4000, 1, 1 << 17) > a
+    # invalid dimensions are refused with 0
+    assert f(0, 4000, 1, 8192) == 0
+    assert f(8, 4000, 6, 8192) == 0
+
+
+def test_noalloc_scratch_is_static(lib):
+    n = lib.eob_noalloc_scratch_bytes()
+    assert n >= lib.eob_workspace_bytes(16, 4096, 1, 8192)
+
+
+def test_product_refuses_without_library(monkeypatch, tmp_path):
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(_lib.EOBError):
+        _lib.load()

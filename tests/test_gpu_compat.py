@@ -30,14 +30,17 @@ def test_hamiltonian_entry_points(torch_cuda, golden):
                                 0.0, 0.0, 0.0, 0.0, n)
     H = out.cpu().numpy()
     ok = np.isfinite(g["H"])
-    # states down to r = 2 with |pr| up to 1.5 are included; there sqrt(A W) is nearly
-    # singular and GPU FMA contraction / libm differences reach ~1e-12
+    # states down to r = 2 with |pr| up to 6 are included; there sqrt(A W) is nearly
+    # singular and GPU FMA contraction / libm differences reach ~1e-12 in H and ~1e-10 in
+    # its gradient.  Away from that corner (r >= 4) the agreement is held to 1e-11.
+    well = ok & (st[0] >= 4.0)
     assert np.max(np.abs(H[ok] / g["H"][ok] - 1)) < 1e-11
     grad = torch.zeros(4 * n, dtype=torch.float64, device="cuda")
     pyEOB.grad_Ham_align_AD(_t(torch, st.ravel()), grad, _t(torch, add.ravel()), n)
     gr = grad.cpu().numpy().reshape(4, n)
-    sc = np.abs(g["grad"][:, ok]).max(axis=0)
-    assert np.max(np.abs(gr[:, ok] - g["grad"][:, ok]) / sc) < 1e-10
+    rel = np.abs(gr - g["grad"]) / np.abs(g["grad"]).max(axis=0)
+    assert np.max(rel[:, ok]) < 1e-9
+    assert np.max(rel[:, well]) < 1e-11
     hess = torch.zeros(16 * n, dtype=torch.float64, device="cuda")
     pyEOB.hessian_Ham_align_AD(_t(torch, st.ravel()), hess, _t(torch, add.ravel()), n)
     hs = hess.cpu().numpy().reshape(16, n)
@@ -70,13 +73,19 @@ def test_ode_and_force(torch_cuda, golden):
         kk = k.cpu().numpy().reshape(4, ns)
         ref = g["rhs"][:, sl]
         ok = np.all(np.isfinite(ref), axis=0)
-        assert np.max(np.abs(kk[:, ok] - ref[:, ok]) / np.abs(ref[:, ok]).max(axis=0)) < 1e-10
+        # near-singular corner (r < 4 with large |pr|) as for the gradient above
+        well = ok & (g["state"][0, sl] >= 4.0)
+        rel = np.abs(kk - ref) / np.abs(ref).max(axis=0)
+        assert np.max(rel[:, ok]) < 1e-9
+        assert np.max(rel[:, well]) < 1e-11
         f = torch.zeros(2 * ns, dtype=torch.float64, device="cuda")
         gbuf = torch.zeros(4 * ns, dtype=torch.float64, device="cuda")
         cls.RR_force(f, gbuf, st, add, ns, idx)
         ff = f.cpu().numpy().reshape(2, ns)
         fr = g["force"][:, sl]
-        assert np.max(np.abs(ff[:, ok] - fr[:, ok]) / np.abs(fr[:, ok]).max(axis=0)) < 1e-10
+        relf = np.abs(ff - fr) / np.abs(fr).max(axis=0)
+        assert np.max(relf[:, ok]) < 1e-9
+        assert np.max(relf[:, well]) < 1e-11
         cls.deallocate_information()
 
 
