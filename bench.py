@@ -239,13 +239,69 @@ def census(args):
     print(json.dumps({"census": wl.counters()}))
 
 
+def run_serving(args, ws, rank, local):
+    """Configuration 4: a seeded Poisson trace of walker requests (1..512
+    binaries each, 80 % from a ball around the injection, 20 % from the
+    configuration-1 prior) replayed in wall-clock time through
+    LikelihoodServer.  The arrival rate is set from a calibration so that the
+    server is about 70 % busy.  Every rank replays its own trace."""
+    import torch
+    from eobgpu_gb300.serving import LikelihoodServer, calibrate_rate
+    cfg = workload.CONFIGS[1]
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    _, data, amp = make_inputs(cfg, rank, device, args.max_steps)
+    lanes = args.lanes or 8
+    server = LikelihoodServer(data, cfg.dt, amp, max_batch=1024, max_steps=args.max_steps, slots=2,
+                              lanes_per_binary=lanes, device=device)
+    trace = workload.serving_trace(args.requests, 1.0, stream=rank)
+    for _ in range(args.warmup):
+        server.evaluate(trace.params[0])
+    rate = calibrate_rate(server, trace.params, busy=0.7)
+    barrier(ws)
+    results = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            results.append(server.run_trace(trace.arrivals, trace.params, time_scale=1.0 / rate))
+    clocks = clk.summary()
+    wall = max_over_ranks(float(sum(r["wall_s"] for r in results)), ws, device)
+    nbin = sum(r["binaries"] for r in results) * ws
+    lat = np.concatenate([r["latency_s"] for r in results])
+    ok = all(np.all(st == 0) for r in results for st in r["status"])
+    if rank == 0:
+        value = nbin / wall
+        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded Poisson trace of walker requests, white noise + one injection at SNR 30",
+                "config": {"workload": "config 4: serving, continuous batching over 2 concurrent slots",
+                           "requests": args.requests, "request_size": [1, 512], "rate_hz": rate,
+                           "target_busy": 0.7, "max_batch": 1024, "slots": 2, "lanes_per_binary": lanes,
+                           "max_steps": args.max_steps, "dt_s": cfg.dt, "n_samples": cfg.n_samples,
+                           "l2": "inputs of each batch are new; no flush (latency run)"},
+                "e2e": {"value": value, "unit": "evals/s",
+                        "h2d_bytes_per_step": int(nbin / ws / args.steps * 40),
+                        "d2h_bytes_per_step": int(nbin / ws / args.steps * 12)},
+                "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
+                "slot_busy_fraction": float(np.mean([r["slot_busy_fraction"] for r in results])),
+                "batches": int(sum(r["batches"] for r in results)),
+                "gpu_launches": int(8 * sum(r["batches"] for r in results)),
+                "roofline": None, "cpu_baseline": None, "clocks": clocks, "status_ok": bool(ok)}
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 5])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
+    ap.add_argument("--fp64", action="store_true", help="configuration 3 in FP64 instead of mixed precision")
+    ap.add_argument("--requests", type=int, default=2000, help="configuration 4: requests in the trace")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--max-steps", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=96)
@@ -254,11 +310,11 @@ def main():
     ap.add_argument("--census", action="store_true",
                     help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
     args = ap.parse_args()
-    cfg = workload.CONFIGS[args.config]
+    cfg = workload.CONFIGS[1 if args.config == 4 else args.config]
     if args.batch:
         cfg = workload.Config(**{**cfg.__dict__, "batch": args.batch})
     if not args.max_steps:
-        args.max_steps = {1: 4000, 2: 6000, 3: 4000, 5: 16000}[args.config]
+        args.max_steps = {1: 4000, 2: 6000, 3: 4000, 4: 4000, 5: 16000}[args.config]
     args.warmup = max(3, args.warmup)
     if args.census:
         census(args)
@@ -270,11 +326,8 @@ def main():
             print(json.dumps(line))
         return
     ws, rank, local = dist_init()
-
-    if args.impl == "reference":
-        line = run_reference(args, cfg, ws, rank)
-        if line is not None:
-            print(json.dumps(line))
+    if args.config == 4:
+        run_serving(args, ws, rank, local)
         return
 
     import torch
@@ -287,14 +340,29 @@ def main():
     from eobgpu_gb300 import _lib
     opt = _lib.default_options()
     opt.lanes_per_binary = args.lanes
-    wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device, options=opt)
+    mixed = args.config == 3 and not args.fp64
+    opt.precision = 1 if mixed else 0
     P = torch.tensor(params, device=device)
     D = torch.tensor(data, device=device)
     order = longest_first(P)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    chunked = None
+    if args.config == 5:
+        from eobgpu_gb300.pipeline import ChunkedLikelihood
+        chunked = ChunkedLikelihood(B, cfg.n_samples, list(cfg.modes), args.max_steps, slots=2, options=opt,
+                                    device=device)
+        wl = chunked.engines[0]
+
+        def run_any(Pd, Od):
+            return chunked.run(Pd, D, cfg.dt, amp)
+    else:
+        wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device, options=opt)
+
+        def run_any(Pd, Od):
+            return wl.run(Pd, D, cfg.dt, amp, order=Od)
 
     def step():
-        return wl.run(P, D, cfg.dt, amp, order=order)
+        return run_any(P, order)
 
     for _ in range(args.warmup):
         lnl, st = step()
@@ -325,7 +393,7 @@ def main():
             ev2[i][0].record()
             Pd = params_h.to(device, non_blocking=True)
             Od = order_h.to(device, non_blocking=True)
-            l_d, s_d = wl.run(Pd, D, cfg.dt, amp, order=Od)
+            l_d, s_d = run_any(Pd, Od)
             lnl_h.copy_(l_d, non_blocking=True)
             st_h.copy_(s_d, non_blocking=True)
             ev2[i][1].record()
@@ -339,21 +407,34 @@ def main():
     status = st.cpu().numpy()
 
     # ---- stage timing and roofline of the integrator (one more untimed step)
+    # (chunked runs: on the first chunk, the longest binaries)
+    if chunked is None:
+        Pst, ordst = P, order
+    else:
+        Pst = P[order[:wl.max_batch].long()].contiguous()
+        ordst = None
+    Bst = int(Pst.shape[0])
     s_ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
     flush.fill_(1.0)
     s_ev[0].record()
-    wl.prepare(P, cfg.dt, order=order, stages=1)
+    wl.prepare(Pst, cfg.dt, order=ordst, stages=1)
     s_ev[1].record()
-    wl.prepare(P, cfg.dt, order=order, stages=2)
+    wl.prepare(Pst, cfg.dt, order=ordst, stages=2)
     s_ev[2].record()
-    wl.prepare(P, cfg.dt, order=order, stages=4)
+    wl.prepare(Pst, cfg.dt, order=ordst, stages=4)
     s_ev[3].record()
-    wl.synth_lnl(B, D, cfg.dt, amp)
+    wl.synth_lnl(Bst, D, cfg.dt, amp)
     s_ev[4].record()
     torch.cuda.synchronize()
     stage_ms = {"setup_ic": s_ev[0].elapsed_time(s_ev[1]), "integrate": s_ev[1].elapsed_time(s_ev[2]),
                 "modes_splines": s_ev[2].elapsed_time(s_ev[3]), "synth_lnl": s_ev[3].elapsed_time(s_ev[4])}
     cnt = wl.counters()
+    # the integrator's critical path: the binary with the most right-hand sides
+    rhs_b = wl.rhs_counts()
+    crit = int(rhs_b.max()) if len(rhs_b) else 0
+    critical = {"binary_rhs_max": crit, "binary_rhs_median": float(np.median(rhs_b)) if len(rhs_b) else 0.0,
+                "rhs_total": int(rhs_b.sum()),
+                "integrate_us_per_rhs_on_path": 1e3 * stage_ms["integrate"] / max(1, crit)}
     # FP64 peak of this device, measured
     nsm = torch.cuda.get_device_properties(device).multi_processor_count
     pk_out = torch.empty(nsm * 8 * 256, dtype=torch.float64, device=device)
@@ -388,15 +469,17 @@ def main():
         launches_per_step = 8  # setup, integrate, scan_rows, modes, spline, scan_chunks, synth, finalize
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_dev / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64 integrator; f64 phase + f32 amplitude/sincos/residual synthesis" if mixed else "f64",
                 "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
-                "config": config_block(cfg, args),
+                "config": config_block(cfg, args, extra=({"chunks": chunked.info(B)} if chunked else None)),
                 "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(B * 5 * 8 + B * 4),
                         "d2h_bytes_per_step": int(B * 8 + B * 4)},
                 "roofline": roof, "cpu_baseline": cpu_base, "clocks": clocks,
                 "gpu_launches": launches_per_step * args.steps,
                 "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
-                "stages_ms": stage_ms, "fp64_peak_tflops": fp64_peak,
+                "stages_ms": stage_ms, "stages_batch": Bst, "critical_path": critical,
+                "fp64_peak_tflops": fp64_peak,
                 "status_ok": int(np.sum(status == 0)), "rows": cnt["rows"]}
         print(json.dumps(line))
     if ws > 1:

@@ -28,7 +28,7 @@ class EobViews(ctypes.Structure):
     _fields_ = [("bins", c_void_p), ("traj", c_void_p), ("nsteps", c_void_p), ("status", c_void_p), ("npts", c_void_p),
                 ("row_off", c_void_p), ("tin", c_void_p), ("spline_y", c_void_p), ("spline_c1", c_void_p),
                 ("spline_c2", c_void_p), ("spline_c3", c_void_p), ("row_capacity", c_int),
-                ("rows_capacity", c_ll), ("nsubs", c_int)]
+                ("rows_capacity", c_ll), ("nsubs", c_int), ("rhs", c_void_p)]
 
 
 # name -> (restype, argtypes); every pointer is passed as an integer address

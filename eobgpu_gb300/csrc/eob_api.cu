@@ -180,6 +180,7 @@ int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_m
     out->row_capacity = max_steps;
     out->rows_capacity = (long long)max_batch * (long long)max_steps;
     out->nsubs = L.nsubs;
+    out->rhs = w.rhs;
     return EOB_OK;
 }
 

@@ -17,6 +17,7 @@ namespace eob {
 // kernel; read-only afterwards).
 struct BinaryRec {
     HamCoeffs ham;
+    HamJets jets;      // the same Hamiltonian as 16 jets for lane groups
     FluxTable flux;
     double pre_re[kNumLM], pre_im[kNumLM];
     double m1s, m2s, chi1, chi2, Mt, omega0, nu;
@@ -29,7 +30,7 @@ constexpr int kChunk = 1024;   // samples per synthesis work item
 constexpr int kTrajStride = 5; // t, r, phi, pr, pphi per trajectory row
 
 struct WsLayout {
-    size_t bins, fac, traj, nsteps, status, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, f32,
+    size_t bins, fac, traj, nsteps, status, rhs, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, f32,
         dataf, total;
     int Bc, Lc, Kc, Nc, nsubs, max_chunks;
 };
@@ -51,6 +52,7 @@ EOB_HD constexpr WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc)
     w.traj = o;      o = align256(o + sizeof(double) * kTrajStride * rows);
     w.nsteps = o;    o = align256(o + sizeof(int) * (size_t)Bc);
     w.status = o;    o = align256(o + sizeof(int) * (size_t)Bc);
+    w.rhs = o;       o = align256(o + sizeof(int) * (size_t)Bc);
     w.queue = o;     o = align256(o + sizeof(unsigned long long) * 8);
     w.row_off = o;   o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
     w.chunk_off = o; o = align256(o + sizeof(long long) * ((size_t)Bc + 1));
@@ -74,6 +76,7 @@ struct Ws {
     FacCoeffs *fac;
     double *traj;
     int *nsteps, *status;
+    int *rhs;                   // right-hand sides evaluated for each binary (both passes, all attempts)
     unsigned long long *queue;  // [0] work queue, [1] total rows, [2] total chunks, [3] sum data^2 (double bits),
                                 // [4] RHS evaluations for binaries, [5] RHS evaluations incl. idle lanes,
                                 // [6] 1 if the spline build wrote FP32 copies (mixed precision)
@@ -94,6 +97,7 @@ inline Ws ws_views(void *base, const WsLayout &L)
     w.traj = (double *)(b + L.traj);
     w.nsteps = (int *)(b + L.nsteps);
     w.status = (int *)(b + L.status);
+    w.rhs = (int *)(b + L.rhs);
     w.queue = (unsigned long long *)(b + L.queue);
     w.row_off = (long long *)(b + L.row_off);
     w.chunk_off = (long long *)(b + L.chunk_off);

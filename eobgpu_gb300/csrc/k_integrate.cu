@@ -102,6 +102,7 @@ struct IntArgs {
     int cap;
     int *nsteps;
     int *status;
+    int *rhs;
     unsigned long long *queue;
     double rtol, atol, h_init, fine_step, step_back, tmax;
     long long max_tries;
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
     bool prevReject = false, fix = false;
     long long tries = 0;
     unsigned long long n_useful = 0, n_all = 0;  // RHS evaluations (census for the roofline)
+    int n_bin = 0;                               // RHS evaluations of the current binary
     const BinaryRec *rec = nullptr;
     double *tr = nullptr;
     bool queue_empty = false;
@@ -145,6 +147,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 st = 0;
                 pass = 1;
                 step = 0;
+                n_bin = 0;
                 x = 0.0;
                 for (int q = 0; q < 4; ++q) y[q] = rec->y0[q];
                 if (leader) {
@@ -162,6 +165,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         if (__all_sync(0xffffffffu, !active)) break;
         n_all += leader ? 1ull : 0ull;
         n_useful += (active && leader) ? 1ull : 0ull;
+        n_bin += active ? 1 : 0;
 
         // ------------------------------------------------ RHS argument
         int out_slot = 1;
@@ -186,7 +190,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         // ------------------------------------------------ the one RHS per loop
         double kk[4];
         if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
-        else eob_rhs_group<G>(rec->ham, rec->flux, arg, kk, sub);
+        else eob_rhs_group<G>(rec->jets, rec->flux, arg, kk, sub);
         if (!active) continue;
 
         // ------------------------------------------------ advance the lane
@@ -320,6 +324,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 if (leader) {
                     a.nsteps[b] = S1 + 1;
                     a.status[b] |= st;
+                    a.rhs[b] = n_bin;
                 }
                 phase = kIdle;
                 continue;
@@ -349,6 +354,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         if (leader) {
             a.nsteps[b] = step + 1;
             a.status[b] |= st;
+            a.rhs[b] = n_bin;
         }
         phase = kIdle;
     }
@@ -367,6 +373,13 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<G>, bs, 0);
         if (per_sm < 1) per_sm = 1;
+        // lane groups: at most one warp per SM sub-partition, so that a long
+        // binary's group never shares the FP64 pipe; later binaries wait in
+        // the queue instead (it hands out the longest first)
+        if (G > 1) {
+            const int cap = (4 * 32 + bs - 1) / bs;
+            if (per_sm > cap) per_sm = cap;
+        }
         const long long lanes = (long long)a.B * G;
         const long long need = (lanes + bs - 1) / bs;
         grid = (int)(need < (long long)nsm * per_sm ? need : (long long)nsm * per_sm);
@@ -401,6 +414,7 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
     a.cap = w.L.Lc;
     a.nsteps = w.nsteps;
     a.status = w.status;
+    a.rhs = w.rhs;
     a.queue = w.queue;
     a.rtol = ra.opt.rtol;
     a.atol = ra.opt.atol;

@@ -41,12 +41,22 @@ __global__ void k_component(const eob::BinaryRec *bins, int iters, double *out)
         } else if (WHICH == 3) {
             const double y[4] = {r, 0.0, pr, L};
             double k[4];
-            eob::eob_rhs_group<16>(b.ham, b.flux, y, k, lane & 15);
+            eob::eob_rhs_group<16>(b.jets, b.flux, y, k, lane & 15);
             acc += k[0] + k[1] + k[2] + k[3];
         } else if (WHICH == 4) {
-            acc += eob::flux_eval_group<16>(b.flux, r, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane & 15);
+            acc += eob::flux_eval_group<16>(b.flux, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane & 15);
         } else if (WHICH == 5) {
-            acc += eob::flux_eval_group<32>(b.flux, r, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane);
+            acc += eob::flux_eval_group<32>(b.flux, L, 0.0227 + 1e-12 * i, 0.987, 0.0226, lane);
+        } else if (WHICH == 6 || WHICH == 7) {
+            eob::HamEval e;
+            if (WHICH == 6) eob::ham_eval_group<16>(b.jets, r, pr, L, lane & 15, &e);
+            else eob::ham_eval_group<32>(b.jets, r, pr, L, lane, &e);
+            acc += e.dHdr + e.dHdpr + e.dHdL + e.omega_c + e.Hreal;
+        } else if (WHICH == 8) {
+            const double y[4] = {r, 0.0, pr, L};
+            double k[4];
+            eob::eob_rhs_group<32>(b.jets, b.flux, y, k, lane);
+            acc += k[0] + k[1] + k[2] + k[3];
         }
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
@@ -64,6 +74,9 @@ extern "C" int eob_component_probe(const void *bins, int which, int iters, doubl
         case 3: k_component<3><<<blocks, threads, 0, stream>>>(b, iters, out); break;
         case 4: k_component<4><<<blocks, threads, 0, stream>>>(b, iters, out); break;
         case 5: k_component<5><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 6: k_component<6><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 7: k_component<7><<<blocks, threads, 0, stream>>>(b, iters, out); break;
+        case 8: k_component<8><<<blocks, threads, 0, stream>>>(b, iters, out); break;
         default: return EOB_E_ARG;
     }
     return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;

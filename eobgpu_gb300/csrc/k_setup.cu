@@ -123,6 +123,7 @@ __device__ void setup_binary(BinaryRec *rec, FacCoeffs *fac, const double *p, do
             newton_prefix(m1s, m2s, l, m, &rec->pre_re[i], &rec->pre_im[i]);
         }
     ham_coeffs_build(&rec->ham, m1s, m2s, chi1, chi2, 0.0, 0.0, 0.0, 0.0);
+    ham_jets_build(rec->ham, &rec->jets);
     flux_table_build(&rec->flux, *fac, rec->pre_re, rec->pre_im, h22_calib, rec->ham.nu);
     rec->m1s = m1s;
     rec->m2s = m2s;
@@ -151,6 +152,7 @@ __global__ void __launch_bounds__(64) k_setup(Ws w, RunArgs a)
     rec->y0[3] = x[1];
     rec->ic_iters = its;
     w.status[i] = st;
+    w.rhs[i] = 0;
 }
 
 cudaError_t launch_setup(const Ws &w, const RunArgs &a, cudaStream_t s)

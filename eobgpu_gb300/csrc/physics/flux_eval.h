@@ -14,6 +14,7 @@
 #pragma once
 #include "fac_coeffs.h"
 #include "ham_eval.h"
+#include "ham_jets.h"
 
 namespace eob {
 
@@ -27,6 +28,7 @@ struct FluxTable {
     double equal_mass;        // 1.0 when eta == 0.25 (odd m use f_lm alone)
     double elog[kLMax + 1];   // gamma + log(2 m), m = 1..8: eulerlog_m(v) = elog[m] + log v
     double gmul[kNumLM];      // m^2 nabs2 / (l!)^2 (lane-group evaluator)
+    double inv2eta;           // 1 / (2 eta) (lane-group evaluator)
 
     EOB_HD double c_rho(int i, int k) const { return rho[i][k]; }
     EOB_HD double c_rhol(int i, int k) const { return rhol[i][k]; }
@@ -88,6 +90,7 @@ EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *pr
     double eta = nu;
     if (eta > 0.25 && eta < 0.25 + 1e-4) eta = 0.25;
     t->eta = eta;
+    t->inv2eta = 0.5 / eta;
     t->equal_mass = (eta == 0.25) ? 1.0 : 0.0;
     t->elog[0] = 0.0;
     for (int m = 1; m <= kLMax; ++m) t->elog[m] = kEulerGamma + log(2.0 * m);
@@ -221,6 +224,24 @@ EOB_HD void lm_of_index(int i, int *l, int *m)
     *m = i + 1;
 }
 
+// Shared pieces of the lane-group flux from v = omega^(1/3) and
+// w = omega_c^(1/3): vPhi = r (omega_c^2 r^3)^(-1/3) omega = omega / w^2
+// (the reference's v_phi, src/EOB.cu:2610-2618, with the r's cancelled).
+EOB_HD FluxShared flux_shared_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+{
+    FluxShared s;
+    s.omega = omega;
+    s.v = v;
+    s.lv = log(v);
+    const double vphi = omega / (w * w);
+    s.vphi2 = vphi * vphi;
+    s.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
+    s.Sodd = v * pphi;
+    s.x = 4.0 * kPi * Hreal * omega;
+    s.E1 = exp(-s.x);
+    return s;
+}
+
 // one multipole of the flux, l and m at run time: m^2 |h_lm|^2 / omega^2
 template <int KMAX>
 EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, double hw)
@@ -313,20 +334,12 @@ __device__ __forceinline__ double flux_rounds(const FluxTable &t, const FluxShar
 }
 
 template <int G>
-__device__ double flux_eval_group(const FluxTable &t, double r, double pphi, double omega, double Hreal, double omega_c,
-                                  int sub)
+__device__ double flux_eval_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
 {
-    FluxShared s;
-    s.omega = omega;
-    s.v = cbrt(omega);
-    s.lv = log(s.v);
-    const double vphi_in = 1.0 / (omega_c * omega_c * r * r * r);
-    const double vphi = r * cbrt(vphi_in) * omega;
-    s.vphi2 = vphi * vphi;
-    s.Se = (Hreal * Hreal - 1.0) / (2.0 * t.eta) + 1.0;
-    s.Sodd = s.v * pphi;
-    s.x = 4.0 * kPi * Hreal * omega;
-    s.E1 = exp(-s.x);
+    // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction
+    const double cr = cbrt((sub & 1) ? omega_c : omega);
+    const FluxShared s = flux_shared_make(t, pphi, omega, Hreal, __shfl_sync(0xffffffffu, cr, 0, G),
+                                          __shfl_sync(0xffffffffu, cr, 1, G));
     double part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
@@ -334,12 +347,12 @@ __device__ double flux_eval_group(const FluxTable &t, double r, double pphi, dou
 }
 
 template <int G>
-__device__ void eob_rhs_group(const HamCoeffs &h, const FluxTable &t, const double y[4], double k[4], int sub)
+__device__ void eob_rhs_group(const HamJets &h, const FluxTable &t, const double y[4], double k[4], int sub)
 {
     HamEval e;
-    ham_eval(h, y[0], y[2], y[3], &e);
+    ham_eval_group<G>(h, y[0], y[2], y[3], sub, &e);
     const double omega = e.dHdL;
-    const double flux = flux_eval_group<G>(t, y[0], y[3], omega, e.Hreal, e.omega_c, sub) / h.nu;
+    const double flux = flux_eval_group<G>(t, y[3], omega, e.Hreal, e.omega_c, sub) / h.nu;
     const double fo = flux / omega;
     k[0] = e.dHdpr;
     k[1] = omega;

@@ -1,0 +1,239 @@
+// The Hamiltonian of ham_eval.h rearranged for a group of lanes that carry one
+// binary: every function of r it needs is one of 16 "jets"
+//
+//   J(u) = sum_k c[k] u^k + log(r) sum_k l[k] u^k + sqrt(u) sum_k s[k] u^k,  k = 0..6,
+//
+// with value and d/du, so that the lanes of a group evaluate different jets
+// with the same instruction stream (no divergence: only the coefficients
+// differ).  The jets are then exchanged by shuffles and every lane runs the
+// combination (A, Bnp, W, the odd part, the square roots).  Lanes of odd index
+// run the combination at p_r = 0, which gives dH/dp_phi at p_r = 0 -- the
+// circular frequency of the flux (src/EOB.cu:2611-2616) -- in the same
+// instructions as the full state on the even lanes.
+//
+// The algebra is that of ham_eval() (same tables, same formulas); only the
+// grouping of the polynomial evaluations differs.
+#pragma once
+#include "ham_eval.h"
+
+namespace eob {
+
+constexpr int kNumJets = 16;
+constexpr int kJetTerms = 7;
+
+enum JetId : int {
+    J_AK0 = 0,  // AK0(u) with its log r and u^6 sqrt(u) terms
+    J_AKA,      // AKa(u)
+    J_FA,       // Fa(u) = 1 + fa1 u + fa2 u^2
+    J_AS,       // AS(u) = 1 + as4 u^4 + as5 u^5 + as6 u^6
+    J_DC,       // Dc(u) = 1 + ap2 u^2 + 2 ap2 u^3
+    J_DB,       // Dbpm(u) with its log r and u^5 sqrt(u) terms
+    J_G,        // 1 + kb u
+    J_BX,       // bs3 u^3 + bs4 u^4 - 1 + ap2 u^2
+    J_BNN,      // -(u^2 + 2 u^3): numerator of Bnpa
+    J_Q4,
+    J_Q6,
+    J_Q8,
+    J_N0,
+    J_N1,
+    J_N2,
+    J_N3,
+};
+
+struct HamJets {
+    double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
+    double n4, apsq, nu, M;
+};
+
+EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
+{
+    for (int j = 0; j < kNumJets; ++j)
+        for (int k = 0; k < kJetTerms; ++k) J->c[j][k] = J->l[j][k] = J->s[j][k] = 0.0;
+    for (int k = 0; k < 7; ++k) {
+        J->c[J_AK0][k] = h.ak0[k];
+        J->c[J_AKA][k] = h.aka[k];
+    }
+    J->l[J_AK0][5] = h.ak0l[5];
+    J->l[J_AK0][6] = h.ak0l[6];
+    J->s[J_AK0][6] = h.ak0h;
+    J->c[J_FA][0] = 1.0;
+    J->c[J_FA][1] = h.fa1;
+    J->c[J_FA][2] = h.fa2;
+    J->c[J_AS][0] = 1.0;
+    J->c[J_AS][4] = h.as4;
+    J->c[J_AS][5] = h.as5;
+    J->c[J_AS][6] = h.as6;
+    J->c[J_DC][0] = 1.0;
+    J->c[J_DC][2] = h.ap2;
+    J->c[J_DC][3] = 2.0 * h.ap2;
+    for (int k = 0; k < 6; ++k) J->c[J_DB][k] = h.db[k];
+    J->l[J_DB][4] = h.dbl[4];
+    J->l[J_DB][5] = h.dbl[5];
+    J->s[J_DB][5] = h.dbh;
+    J->c[J_G][0] = 1.0;
+    J->c[J_G][1] = h.kb;
+    J->c[J_BX][0] = -1.0;
+    J->c[J_BX][2] = h.ap2;
+    J->c[J_BX][3] = h.bs3;
+    J->c[J_BX][4] = h.bs4;
+    J->c[J_BNN][2] = -1.0;
+    J->c[J_BNN][3] = -2.0;
+    for (int k = 2; k <= 4; ++k) J->c[J_Q4][k] = h.q4c[k];
+    J->l[J_Q4][4] = h.q4l;
+    J->s[J_Q4][4] = h.q4h;
+    J->c[J_Q6][2] = h.q6c[2];
+    J->c[J_Q6][3] = h.q6c[3];
+    J->s[J_Q6][3] = h.q6h;
+    J->c[J_Q8][1] = h.q8c[1];
+    J->c[J_Q8][2] = h.q8c[2];
+    J->s[J_Q8][2] = h.q8h;
+    for (int k = 0; k <= 4; ++k) J->c[J_N0][k] = h.nc[0][k];
+    J->l[J_N0][4] = h.ncl[0][4];
+    for (int k = 0; k <= 3; ++k) J->c[J_N1][k] = h.nc[1][k];
+    J->l[J_N1][3] = h.ncl[1][3];
+    for (int k = 0; k <= 2; ++k) J->c[J_N2][k] = h.nc[2][k];
+    for (int k = 0; k <= 1; ++k) J->c[J_N3][k] = h.nc[3][k];
+    J->n4 = h.nc[4][0];
+    J->apsq = h.apsq;
+    J->nu = h.nu;
+    J->M = h.M;
+}
+
+// value and d/du of jet j at u (r = 1/u, lr = log r, su = sqrt(u))
+EOB_HD Jet jet_eval(const HamJets &J, int j, double u, double r, double lr, double su)
+{
+    const double *c = J.c[j], *l = J.l[j], *s = J.s[j];
+    double cv = c[6], cd = 0.0, lv = l[6], ld = 0.0, sv = s[6], sd = 0.0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        cd = fma(cd, u, cv);
+        cv = fma(cv, u, c[k]);
+        ld = fma(ld, u, lv);
+        lv = fma(lv, u, l[k]);
+        sd = fma(sd, u, sv);
+        sv = fma(sv, u, s[k]);
+    }
+    // d(log r)/du = -r, d(sqrt u)/du = sqrt(u) r / 2
+    Jet out;
+    out.v = fma(su, sv, fma(lr, lv, cv));
+    out.d = fma(su, fma(0.5 * r, sv, sd), fma(lr, ld, fma(-r, lv, cd)));
+    return out;
+}
+
+// H and its first derivatives at (r, pr, L) from the 16 jets
+struct HamPart {
+    double H, Hreal, dHdr, dHdpr, dHdL;
+};
+
+EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr, double L)
+{
+    const Jet ak0 = jt[J_AK0], aka = jt[J_AKA], fa = jt[J_FA], as = jt[J_AS], dc = jt[J_DC], db = jt[J_DB],
+              g = jt[J_G], bx = jt[J_BX], bnn = jt[J_BNN], q4 = jt[J_Q4], q6 = jt[J_Q6], q8 = jt[J_Q8],
+              n0 = jt[J_N0], n1 = jt[J_N1], n2 = jt[J_N2], n3 = jt[J_N3];
+    const double u2 = u * u, u3 = u2 * u;
+    const double idc = 1.0 / dc.v;
+    const double Sv = ak0.v + aka.v, Sd = ak0.d + aka.d;
+    const double sf = Sv * fa.v;
+    const double na = sf * as.v;
+    const double dna = fma(Sd * fa.v + Sv * fa.d, as.v, sf * as.d);
+    const double Av = na * idc;
+    const double Ad = fma(-Av, dc.d, dna) * idc;
+
+    const double ad = ak0.v * db.v;
+    const double bnpv = fma(ad, g.v, bx.v);
+    const double bnpd = fma(fma(ak0.d, db.v, ak0.v * db.d), g.v, fma(ad, g.d, bx.d));
+    const double bnpa = bnn.v * idc;
+    const double dbnpa = fma(-bnpa, dc.d, bnn.d) * idc;
+    const double cf = fma(J.apsq, bnpa, 1.0);
+    const double cuv = u2 * cf;
+    const double cud = fma(2.0 * u, cf, u2 * J.apsq * dbnpa);
+
+    const double p2 = pr * pr, L2 = L * L;
+    const double qa = fma(p2, fma(p2, q8.v, q6.v), q4.v);
+    const double qad = fma(p2, fma(p2, q8.d, q6.d), q4.d);
+    const double W = 1.0 + p2 * (1.0 + bnpv) + L2 * cuv + p2 * p2 * qa;
+    const double Wu = p2 * bnpd + L2 * cud + p2 * p2 * qad;
+    const double Wp = 2.0 * pr * ((1.0 + bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
+    const double WL = 2.0 * L * cuv;
+
+    const double heven = sqrt(Av * W);
+    const double ih2 = 0.5 / heven;
+    const double hev_u = fma(Ad, W, Av * Wu) * ih2;
+    const double hev_p = Av * Wp * ih2;
+    const double hev_L = Av * WL * ih2;
+
+    const double n4 = J.n4;
+    const double Nv = n0.v + p2 * (n1.v + p2 * (n2.v + p2 * (n3.v + p2 * n4)));
+    const double Nu = n0.d + p2 * (n1.d + p2 * (n2.d + p2 * n3.d));
+    const double Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * 4.0 * n4));
+    const double u3i = u3 * idc;
+    const double hodd = L * u3i * Nv;
+    const double hodd_u = L * idc * (3.0 * u2 * Nv + u3 * Nu - u3 * Nv * idc * dc.d);
+    const double hodd_p = L * u3i * Np * 2.0 * pr;
+    const double hodd_L = u3i * Nv;
+
+    const double heff = heven + hodd;
+    const double nu = J.nu, M = J.M;
+    const double s = sqrt(1.0 + 2.0 * nu * (heff - 1.0));
+    const double f = M / s;
+    HamPart o;
+    o.H = M * s / nu;
+    o.Hreal = M * s;
+    o.dHdr = -u2 * f * (hev_u + hodd_u);
+    o.dHdpr = f * (hev_p + hodd_p);
+    o.dHdL = f * (hev_L + hodd_L);
+    return o;
+}
+
+// Sequential use of the same pieces (host tests, and one-lane callers)
+EOB_HD void ham_eval_jets(const HamJets &J, double r, double pr, double L, HamEval *out)
+{
+    const double u = 1.0 / r, lr = log(r), su = sqrt(u);
+    Jet jt[kNumJets];
+    for (int j = 0; j < kNumJets; ++j) jt[j] = jet_eval(J, j, u, r, lr, su);
+    const HamPart a = ham_combine(J, jt, u, pr, L);
+    const HamPart c = ham_combine(J, jt, u, 0.0, L);
+    out->H = a.H;
+    out->Hreal = a.Hreal;
+    out->dHdr = a.dHdr;
+    out->dHdpr = a.dHdpr;
+    out->dHdL = a.dHdL;
+    out->omega_c = c.dHdL;
+}
+
+#ifdef __CUDACC__
+// G lanes (2 .. 32, power of two) of one binary: jets split over the lanes,
+// full state on even lanes and p_r = 0 on odd lanes; every lane returns the
+// same result.  All 32 lanes of the warp must call it together.
+template <int G>
+__device__ __forceinline__ void ham_eval_group(const HamJets &J, double r, double pr, double L, int sub,
+                                               HamEval *out)
+{
+    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0, "group size");
+    const double u = 1.0 / r, lr = log(r), su = sqrt(u);
+    constexpr int R = (kNumJets + G - 1) / G;
+    double mv[R], md[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        const int j = (q * G + sub) & (kNumJets - 1);
+        const Jet t = jet_eval(J, j, u, r, lr, su);
+        mv[q] = t.v;
+        md[q] = t.d;
+    }
+    Jet jt[kNumJets];
+#pragma unroll
+    for (int j = 0; j < kNumJets; ++j) {
+        jt[j].v = __shfl_sync(0xffffffffu, mv[j / G], j % G, G);
+        jt[j].d = __shfl_sync(0xffffffffu, md[j / G], j % G, G);
+    }
+    const HamPart p = ham_combine(J, jt, u, (sub & 1) ? 0.0 : pr, L);
+    out->H = __shfl_sync(0xffffffffu, p.H, 0, G);
+    out->Hreal = __shfl_sync(0xffffffffu, p.Hreal, 0, G);
+    out->dHdr = __shfl_sync(0xffffffffu, p.dHdr, 0, G);
+    out->dHdpr = __shfl_sync(0xffffffffu, p.dHdpr, 0, G);
+    out->dHdL = __shfl_sync(0xffffffffu, p.dHdL, 0, G);
+    out->omega_c = __shfl_sync(0xffffffffu, p.dHdL, 1, G);
+}
+#endif
+
+}  // namespace eob

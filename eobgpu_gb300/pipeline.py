@@ -169,6 +169,12 @@ class WaveformLikelihood:
                    "eob_workspace_counters")
         return {"rows": int(buf[1]), "chunks": int(buf[2]), "rhs_binaries": int(buf[4]), "rhs_all_lanes": int(buf[5])}
 
+    def rhs_counts(self):
+        """Right-hand sides evaluated per binary in the last run (host numpy)."""
+        torch.cuda.synchronize()
+        v = self.views()
+        return self._dev_array(v.rhs, self.last_B, torch.int32).cpu().numpy()
+
     def npts(self):
         torch.cuda.synchronize()
         v = self.views()
@@ -212,3 +218,82 @@ class WaveformLikelihood:
         traj = self._dev_array(v.traj, self.last_B * self.max_steps * 5, torch.float64).view(-1, self.max_steps, 5)
         first = traj[:, 0].cpu().numpy()
         return np.stack([first[:, 1], first[:, 4], first[:, 3]], axis=1)
+
+
+def chunk_size_for_budget(budget_bytes: int, max_steps: int, n_modes: int, n_samples: int, upper: int) -> int:
+    """Largest batch whose workspace fits in budget_bytes (0 if none does)."""
+    lib = _lib.load()
+    lo, hi = 0, int(upper)
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        need = int(lib.eob_workspace_bytes(mid, int(max_steps), int(n_modes), int(n_samples)))
+        if need != 0 and need <= budget_bytes:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
+
+
+class ChunkedLikelihood:
+    """lnL of batches larger than one workspace, in memory-admitted chunks.
+
+    Chunks are sized so that `slots` workspaces fit in hbm_budget_bytes
+    (default: 60 % of the free device memory) for batches of up to
+    max_batch binaries; a call orders its batch longest first, cuts it into
+    chunks and alternates them over the slots' streams, so that a chunk
+    starts while the ragged tail of the previous one still runs."""
+
+    def __init__(self, max_batch: int, n_samples: int, modes=((2, 2),), max_steps: int = 16000,
+                 hbm_budget_bytes: int | None = None, slots: int = 2, options: _lib.EobOptions | None = None,
+                 device="cuda"):
+        self.device = torch.device(device)
+        if hbm_budget_bytes is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget_bytes = int(0.6 * free)
+        self.budget = int(hbm_budget_bytes)
+        per_slot = self.budget // max(1, slots)
+        self.chunk = chunk_size_for_budget(per_slot, max_steps, len(modes), n_samples, max(1, -(-max_batch // slots)))
+        if self.chunk < 1:
+            raise _lib.EOBError(f"HBM budget {self.budget} B admits no binary at max_steps={max_steps}, "
+                                f"N={n_samples}")
+        nslots = min(slots, -(-max_batch // self.chunk))
+        self.engines = [WaveformLikelihood(self.chunk, max_steps, modes, n_samples, device=self.device,
+                                           options=options) for _ in range(nslots)]
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(nslots)]
+        self.identity = torch.arange(self.chunk, dtype=torch.int32, device=self.device)
+
+    def info(self, B: int):
+        return {"chunk": self.chunk, "chunks": -(-B // self.chunk), "slots": len(self.engines),
+                "workspace_bytes_per_slot": self.engines[0].ws_bytes, "budget_bytes": self.budget}
+
+    def run(self, params: torch.Tensor, data: torch.Tensor, dt: float, amp: float):
+        B = int(params.shape[0])
+        order = longest_first(params).long()
+        lnl = torch.empty(B, dtype=torch.float64, device=self.device)
+        status = torch.empty(B, dtype=torch.int32, device=self.device)
+        main = torch.cuda.current_stream(self.device)
+        n = len(self.engines)
+        for j, lo in enumerate(range(0, B, self.chunk)):
+            e, s = self.engines[j % n], self.streams[j % n]
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                idx = order[lo:lo + self.chunk]
+                P = params[idx].contiguous()
+                l, st = e.run(P, data, dt, amp, order=self.identity[:len(idx)], stream=s)
+                lnl[idx] = l
+                status[idx] = st
+                for t in (P, l, st, idx):
+                    t.record_stream(s)
+        for s in self.streams:
+            main.wait_stream(s)
+        return lnl, status
+
+
+def lnl_chunked(params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, modes=((2, 2),),
+                max_steps: int = 16000, hbm_budget_bytes: int | None = None, slots: int = 2,
+                options: _lib.EobOptions | None = None, device="cuda"):
+    """One-shot ChunkedLikelihood: (lnl, status, info) in the input order."""
+    c = ChunkedLikelihood(int(params.shape[0]), int(data.shape[0]), modes, max_steps, hbm_budget_bytes, slots,
+                          options, device)
+    lnl, status = c.run(params, data, dt, amp)
+    return lnl, status, c.info(int(params.shape[0]))

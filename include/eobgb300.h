@@ -138,6 +138,7 @@ typedef struct eob_views {
     int row_capacity;     /* max_steps */
     long long rows_capacity;
     int nsubs;
+    int *rhs;             /* right-hand sides evaluated per binary (both passes, every attempt) */
 } eob_views;
 int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
                         eob_views *out);
@@ -155,7 +156,8 @@ int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t
 /* Timing probe of one piece of the right-hand side on binary 0 of a prepared
  * workspace (bins from eob_workspace_views): which = 0 Hamiltonian and
  * gradient, 1 flux, 2 right-hand side, 3 right-hand side with 16 lanes per
- * binary, 4 flux with 16 lanes, 5 flux with 32 lanes. */
+ * binary, 4 flux with 16 lanes, 5 flux with 32 lanes, 6 Hamiltonian with 16
+ * lanes, 7 Hamiltonian with 32 lanes, 8 right-hand side with 32 lanes. */
 int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
                         cudaStream_t stream);
 

@@ -4,6 +4,7 @@
 #include "../../eobgpu_gb300/csrc/physics/fac_coeffs.h"
 #include "../../eobgpu_gb300/csrc/physics/ham_coeffs.h"
 #include "../../eobgpu_gb300/csrc/physics/ham_eval.h"
+#include "../../eobgpu_gb300/csrc/physics/ham_jets.h"
 #include "../../eobgpu_gb300/csrc/physics/flux_eval.h"
 
 extern "C" {
@@ -17,6 +18,22 @@ void phys_ham(const double *st, const double *add, int n, double *out)
                               add[7 * n + i], add[8 * n + i]);
         eob::HamEval e;
         eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
+        out[5 * i + 0] = e.H; out[5 * i + 1] = e.dHdr; out[5 * i + 2] = e.dHdpr; out[5 * i + 3] = e.dHdL;
+        out[5 * i + 4] = e.omega_c;
+    }
+}
+
+// the same through the 16-jet form used by lane groups (ham_jets.h)
+void phys_ham_jets(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, add[i], add[n + i], add[2 * n + i], add[3 * n + i], add[5 * n + i], add[6 * n + i],
+                              add[7 * n + i], add[8 * n + i]);
+        eob::HamJets J;
+        eob::ham_jets_build(h, &J);
+        eob::HamEval e;
+        eob::ham_eval_jets(J, st[i], st[2 * n + i], st[3 * n + i], &e);
         out[5 * i + 0] = e.H; out[5 * i + 1] = e.dHdr; out[5 * i + 2] = e.dHdpr; out[5 * i + 3] = e.dHdL;
         out[5 * i + 4] = e.omega_c;
     }
@@ -45,7 +62,8 @@ void phys_rhs(const double *st, const double *add, int n, double *k)
     }
 }
 
-// flux two ways: specialised per-mode code and the generic lane-group mode evaluator
+// flux three ways: specialised per-mode code, the generic lane-group mode
+// evaluator, and the same with the lane-group shared pieces
 void phys_flux_both(const double *st, const double *add, int n, double *out)
 {
     for (int i = 0; i < n; ++i) {
@@ -64,7 +82,7 @@ void phys_flux_both(const double *st, const double *add, int n, double *out)
         eob::HamEval e;
         eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
         const double omega = e.dHdL;
-        out[2 * i] = eob::flux_eval(t, st[i], st[3 * n + i], omega, e.Hreal, e.omega_c);
+        out[3 * i] = eob::flux_eval(t, st[i], st[3 * n + i], omega, e.Hreal, e.omega_c);
         eob::FluxShared s;
         s.omega = omega;
         s.v = cbrt(omega);
@@ -77,7 +95,12 @@ void phys_flux_both(const double *st, const double *add, int n, double *out)
         s.E1 = exp(-s.x);
         double sum = 0.0;
         for (int j = 0; j < 35; ++j) sum += eob::flux_mode_generic<10>(t, j, s, e.Hreal * omega);
-        out[2 * i + 1] = sum * omega * omega / (8.0 * eob::kPi);
+        out[3 * i + 1] = sum * omega * omega / (8.0 * eob::kPi);
+        // the lane-group form: shared pieces from the two cube roots
+        const eob::FluxShared s2 = eob::flux_shared_make(t, st[3 * n + i], omega, e.Hreal, cbrt(omega), cbrt(e.omega_c));
+        double sum2 = 0.0;
+        for (int j = 0; j < 35; ++j) sum2 += eob::flux_mode_generic<10>(t, j, s2, e.Hreal * omega);
+        out[3 * i + 2] = sum2 * omega * omega / (8.0 * eob::kPi);
     }
 }
 

@@ -43,8 +43,8 @@ def test_struct_layouts_match_header(lib):
 int main(void) {
   printf("%zu %zu %zu %zu %zu\n", sizeof(eob_options), offsetof(eob_options, ic_mode),
          offsetof(eob_options, max_tries), offsetof(eob_options, lanes_per_binary), sizeof(eob_views));
-  printf("%zu %zu %zu\n", offsetof(eob_views, row_capacity), offsetof(eob_views, rows_capacity),
-         offsetof(eob_views, nsubs));
+  printf("%zu %zu %zu %zu\n", offsetof(eob_views, row_capacity), offsetof(eob_views, rows_capacity),
+         offsetof(eob_views, nsubs), offsetof(eob_views, rhs));
   return 0;
 }
 """
@@ -59,7 +59,7 @@ int main(void) {
         out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
     o, v = _lib.EobOptions, _lib.EobViews
     want = [ctypes.sizeof(o), o.ic_mode.offset, o.max_tries.offset, o.lanes_per_binary.offset, ctypes.sizeof(v),
-            v.row_capacity.offset, v.rows_capacity.offset, v.nsubs.offset]
+            v.row_capacity.offset, v.rows_capacity.offset, v.nsubs.offset, v.rhs.offset]
     assert [int(x) for x in out] == want
 
 
@@ -94,3 +94,13 @@ def test_product_refuses_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(_lib.EOBError):
         _lib.load()
+
+
+def test_chunk_size_for_budget(lib):
+    from eobgpu_gb300.pipeline import chunk_size_for_budget
+    f = lib.eob_workspace_bytes
+    for B in (1, 7, 100, 4096):
+        budget = f(B, 16000, 1, 1 << 20)
+        assert chunk_size_for_budget(budget, 16000, 1, 1 << 20, 10 ** 6) == B
+        assert chunk_size_for_budget(budget - 1, 16000, 1, 1 << 20, 10 ** 6) == B - 1
+    assert chunk_size_for_budget(10, 16000, 1, 1 << 20, 100) == 0

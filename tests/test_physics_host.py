@@ -42,6 +42,32 @@ def test_ham_eval_vs_reference(phys, golden):
         assert np.max(np.abs(out[j][ok] - gr[q][ok]) / sc) < 1e-12
 
 
+def test_ham_jets_match_ham_eval(phys, golden):
+    """The 16-jet arrangement used by lane groups against the sequential
+    evaluation and the reference."""
+    g = golden["ham_rhs"]
+    st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
+    n = st.shape[1]
+    a = np.zeros(5 * n)
+    b = np.zeros(5 * n)
+    phys.phys_ham(dp(st), dp(add), ctypes.c_int(n), dp(a))
+    phys.phys_ham_jets(dp(st), dp(add), ctypes.c_int(n), dp(b))
+    a, b = a.reshape(n, 5).T, b.reshape(n, 5).T
+    ok = np.all(np.isfinite(a), axis=0)
+    np.testing.assert_array_equal(np.all(np.isfinite(b), axis=0), ok)
+    well = ok & (st[0] >= 4.0)
+    for j in range(5):
+        sc = np.abs(a[1:4]).max(axis=0) if 1 <= j <= 3 else np.abs(a[j])
+        rel = np.abs(b[j] - a[j]) / sc
+        assert np.max(rel[ok]) < 1e-11, j
+        assert np.max(rel[well]) < 1e-13, j
+    gr = g["grad"]
+    sc = np.abs(gr[:, ok]).max(axis=0)
+    assert np.max(np.abs(b[0][ok] / g["H"][ok] - 1)) < 1e-13
+    for j, q in ((1, 0), (2, 2), (3, 3)):
+        assert np.max(np.abs(b[j][ok] - gr[q][ok]) / sc) < 1e-12
+
+
 def test_rhs_vs_reference(phys, golden):
     g = golden["ham_rhs"]
     st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
@@ -59,12 +85,13 @@ def test_generic_flux_matches_specialised(phys, golden):
     g = golden["ham_rhs"]
     st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
     n = st.shape[1]
-    out = np.zeros(2 * n)
+    out = np.zeros(3 * n)
     phys.phys_flux_both(dp(st), dp(add), ctypes.c_int(n), dp(out))
-    out = out.reshape(n, 2)
+    out = out.reshape(n, 3)
     ok = np.isfinite(out[:, 0])
     assert ok.sum() > 0.9 * n
     assert np.max(np.abs(out[ok, 1] / out[ok, 0] - 1)) < 1e-13
+    assert np.max(np.abs(out[ok, 2] / out[ok, 0] - 1)) < 1e-13
 
 
 def test_newton_prefixes(phys):
