@@ -389,16 +389,19 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// Lanes per binary: enough lanes for about one warp per SM sub-partition,
-// power of two in [1, 32].  One lane per binary is the most efficient use of
-// the FP64 pipe; more lanes per binary shorten each binary's critical path
-// when the batch cannot fill the device.
+// Lanes per binary: a power of two in [1, 32].  One lane per binary is the
+// most efficient use of the FP64 pipe; more lanes per binary shorten each
+// binary's critical path when the batch cannot fill the device.
 int auto_lanes_per_binary(int B)
 {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const long long target = (long long)nsm * 4 * 32;
+    // up to two warps' worth of lanes per SM sub-partition: the grid keeps one
+    // warp per sub-partition resident and the work queue feeds it the rest,
+    // longest binaries first, so a batch bound by its longest binary gets the
+    // shortest chain (e.g. B = 1024 -> 32 lanes, B = 4096 -> 8 lanes)
+    const long long target = (long long)nsm * 4 * 32 * 2;
     int G = 1;
     while (G < 32 && (long long)B * (G * 2) <= target) G *= 2;
     return G;

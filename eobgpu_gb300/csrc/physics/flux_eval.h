@@ -258,7 +258,7 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
         rho = (rho + ck) * s.v;
     }
     rho += 1.0;
-    if (i == 0) {
+    if (i == lm_index(2, 2)) {
         const double v4 = (s.v * s.v) * (s.v * s.v);
         rho = fma(t.h22calib, v4 * v4 * v4, rho);
     }
@@ -297,6 +297,152 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
 }
 
 
+// ---------------------------------------------------------------------------
+// Multipole evaluation for lane groups of 8 or more lanes.  The factors that
+// depend on m only are computed once per call on lanes 0..7 of the group (one
+// exp(-m x) and one division per lane, in one instruction stream) and read by
+// shuffles; the Gamma product prod_{j<=l} (4 k^2 + j^2) is a polynomial in
+// 4 k^2 from a table; powers of v_phi^2 are precomputed and selected.
+
+// prod_{j=1..l} (x + j^2) = sum_i kTprod[l][i] x^i (exact integers)
+#define EOB_TPROD_INIT                                                                                       \
+    {{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {4.0, 5.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {36.0, 49.0, 14.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                       \
+     {576.0, 820.0, 273.0, 30.0, 1.0, 0.0, 0.0, 0.0, 0.0},                                                   \
+     {14400.0, 21076.0, 7645.0, 1023.0, 55.0, 1.0, 0.0, 0.0, 0.0},                                           \
+     {518400.0, 773136.0, 296296.0, 44473.0, 3003.0, 91.0, 1.0, 0.0, 0.0},                                   \
+     {25401600.0, 38402064.0, 15291640.0, 2475473.0, 191620.0, 7462.0, 140.0, 1.0, 0.0},                    \
+     {1625702400.0, 2483133696.0, 1017067024.0, 173721912.0, 14739153.0, 669188.0, 16422.0, 204.0, 1.0}}
+static constexpr double kTprodH[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
+#ifdef __CUDACC__
+__device__ const double kTprodD[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
+#endif
+
+EOB_HD const double *tprod_row(int l)
+{
+#ifdef __CUDA_ARCH__
+    return kTprodD[l];
+#else
+    return kTprodH[l];
+#endif
+}
+
+// per-call pieces shared by every multipole of one lane group
+struct FluxLane {
+    double v, lv, v12, Se, Sodd;
+    double vp[8];  // vphi^(2 e), e = 2..9
+};
+
+EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+{
+    FluxLane f;
+    f.v = v;
+    f.lv = log(v);
+    const double v2 = v * v, v4 = v2 * v2;
+    f.v12 = v4 * v4 * v4;
+    const double vphi = omega / (w * w);
+    const double p1 = vphi * vphi;
+    const double p2 = p1 * p1, p3 = p2 * p1, p4 = p2 * p2;
+    f.vp[0] = p2;
+    f.vp[1] = p3;
+    f.vp[2] = p4;
+    f.vp[3] = p4 * p1;
+    f.vp[4] = p3 * p3;
+    f.vp[5] = p3 * p4;
+    f.vp[6] = p4 * p4;
+    f.vp[7] = p4 * p4 * p1;
+    f.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
+    f.Sodd = v * pphi;
+    return f;
+}
+
+// m x / (1 - e^{-m x}) and 4 k^2 = 4 (m H omega)^2 for one m
+EOB_HD void flux_m_factors(int m, double x, double hw, double *T, double *k4)
+{
+    const double xm = m * x;
+    *T = xm / (1.0 - exp(-xm));
+    const double km = m * hw;
+    *k4 = 4.0 * km * km;
+}
+
+// l and m of lm_index i, packed (l << 4) | m
+#define EOB_LM_INIT                                                                                          \
+    {0x21, 0x22, 0x31, 0x32, 0x33, 0x41, 0x42, 0x43, 0x44, 0x51, 0x52, 0x53, 0x54, 0x55, 0x61, 0x62, 0x63, 0x64, \
+     0x65, 0x66, 0x71, 0x72, 0x73, 0x74, 0x75, 0x76, 0x77, 0x81, 0x82, 0x83, 0x84, 0x85, 0x86, 0x87, 0x88}
+
+static constexpr unsigned char kLMH[kNumLM] = EOB_LM_INIT;
+#ifdef __CUDACC__
+__device__ const unsigned char kLMD[kNumLM] = EOB_LM_INIT;
+#endif
+
+EOB_HD int lm_packed(int i)
+{
+#ifdef __CUDA_ARCH__
+    return kLMD[i];
+#else
+    return kLMH[i];
+#endif
+}
+
+// m^2 |h_lm|^2 / omega^2 of multipole i (rho_lm series of at most KMAX
+// terms) from the shared pieces and the m factors T, k4 of its m
+template <int KMAX>
+EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
+{
+    const int lm = lm_packed(i);
+    const int l = lm >> 4, m = lm & 15;
+    const int eps = (l + m) & 1;
+    const double elm = t.elog[m] + f.lv;
+    // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
+    double acc = t.rho[i][KMAX];
+    if (KMAX == 6 || KMAX == 7 || KMAX == 8 || KMAX == 10) acc = fma(t.rhol[i][KMAX], elm, acc);
+#pragma unroll
+    for (int k = KMAX - 1; k >= 1; --k) {
+        double ck = t.rho[i][k];
+        if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
+        acc = fma(acc, f.v, ck);
+    }
+    double rho = fma(acc, f.v, 1.0);
+    rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
+    // rho^l by squaring (l = 2..8)
+    const double r2 = rho * rho, r4 = r2 * r2;
+    double rpl = (l & 4) ? r4 : 1.0;
+    if (l & 2) rpl *= r2;
+    if (l & 1) rpl *= rho;
+    if (l == 8) rpl = r4 * r4;
+    const double aux = f.v * fma(t.f3[i], f.v * f.v, t.f1[i]);
+    rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
+    const double S = eps ? f.Sodd : f.Se;
+    // vphi^(2 (l + eps)) selected from the precomputed powers
+    const int e = l + eps - 2;
+    double vpw = f.vp[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) vpw = (e == q) ? f.vp[q] : vpw;
+    // prod_{j<=l} (4 k^2 + j^2)
+    const double *c = tprod_row(l);
+    double P = c[kLMax];
+#pragma unroll
+    for (int q = kLMax - 1; q >= 0; --q) P = fma(P, k4, c[q]);
+    return t.gmul[i] * T * P * (S * S) * (rpl * rpl) * vpw;
+}
+
+// Sequential use of the lane-group pieces (host tests)
+EOB_HD double flux_eval_lanes(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c)
+{
+    const FluxLane f = flux_lane_make(t, pphi, omega, Hreal, cbrt(omega), cbrt(omega_c));
+    const double x = 4.0 * kPi * Hreal * omega, hw = Hreal * omega;
+    double T[kLMax + 1], k4[kLMax + 1];
+    for (int m = 1; m <= kLMax; ++m) flux_m_factors(m, x, hw, &T[m], &k4[m]);
+    double sum = 0.0;
+    for (int i = 0; i < kNumLM; ++i) {
+        const int m = lm_packed(i) & 15;
+        sum += flux_mode_lane<10>(t, i, f, T[m], k4[m]);
+    }
+    return sum * omega * omega / (8.0 * kPi);
+}
+
 #ifdef __CUDACC__
 // ---------------------------------------------------------------------------
 // The same flux with the 35 multipoles spread over a group of G lanes that
@@ -307,8 +453,9 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
 // The partial sums are combined with butterfly shuffles inside the group.
 
 // slot (lm_index) of the modes ordered by flux rho degree, longest first
-__device__ __constant__ signed char kFluxOrder[kNumLM] = {
-    0, 1,                                  // (2,2) (2,1): degree 10
+// (global memory, not __constant__: the lanes of a warp read different entries)
+__device__ const signed char kFluxOrder[kNumLM] = {
+    0, 1,                                  // (2,1) (2,2): degree 10
     4, 3, 2,                               // (3,3) (3,2) (3,1): 8
     8, 7, 6, 5, 13,                        // (4,4..1) (5,5): 6
     11, 9,                                 // (5,3) (5,1): 5
@@ -333,14 +480,43 @@ __device__ __forceinline__ double flux_rounds(const FluxTable &t, const FluxShar
     }
 }
 
+template <int G, int R>
+__device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const FluxLane &f, double Tm, double k4m,
+                                                   int sub)
+{
+    constexpr int first = R * G;
+    if constexpr (first >= kNumLM) {
+        return 0.0;
+    } else {
+        constexpr int KM = kFluxDegSorted[first];
+        const int pos = first + sub;
+        const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
+        const int m = lm_packed(i) & 15;
+        // the m factors live on lanes m-1 of the group
+        const double T = __shfl_sync(0xffffffffu, Tm, m - 1, G);
+        const double k4 = __shfl_sync(0xffffffffu, k4m, m - 1, G);
+        double here = flux_mode_lane<KM>(t, i, f, T, k4);
+        if (pos >= kNumLM) here = 0.0;
+        return here + flux_rounds_lane<G, R + 1>(t, f, Tm, k4m, sub);
+    }
+}
+
 template <int G>
 __device__ double flux_eval_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
 {
     // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction
     const double cr = cbrt((sub & 1) ? omega_c : omega);
-    const FluxShared s = flux_shared_make(t, pphi, omega, Hreal, __shfl_sync(0xffffffffu, cr, 0, G),
-                                          __shfl_sync(0xffffffffu, cr, 1, G));
-    double part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
+    const double v = __shfl_sync(0xffffffffu, cr, 0, G), w = __shfl_sync(0xffffffffu, cr, 1, G);
+    double part;
+    if constexpr (G >= 8) {
+        const FluxLane f = flux_lane_make(t, pphi, omega, Hreal, v, w);
+        double Tm, k4m;
+        flux_m_factors((sub & 7) + 1, 4.0 * kPi * Hreal * omega, Hreal * omega, &Tm, &k4m);
+        part = flux_rounds_lane<G, 0>(t, f, Tm, k4m, sub);
+    } else {
+        const FluxShared s = flux_shared_make(t, pphi, omega, Hreal, v, w);
+        part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
+    }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
     return part * omega * omega / (8.0 * kPi);

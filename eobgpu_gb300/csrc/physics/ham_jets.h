@@ -40,6 +40,17 @@ enum JetId : int {
     J_N3,
 };
 
+// 1/sqrt(x): the device's reciprocal square root (one instruction sequence
+// instead of a square root and a division); on the host 1/sqrt(x)
+EOB_HD double eob_rsqrt(double x)
+{
+#ifdef __CUDA_ARCH__
+    return rsqrt(x);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
 struct HamJets {
     double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
     double n4, apsq, nu, M;
@@ -156,8 +167,11 @@ EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr,
     const double Wp = 2.0 * pr * ((1.0 + bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
     const double WL = 2.0 * L * cuv;
 
-    const double heven = sqrt(Av * W);
-    const double ih2 = 0.5 / heven;
+    // sqrt and the reciprocal from one reciprocal square root
+    const double AW = Av * W;
+    const double rAW = eob_rsqrt(AW);
+    const double heven = AW * rAW;
+    const double ih2 = 0.5 * rAW;
     const double hev_u = fma(Ad, W, Av * Wu) * ih2;
     const double hev_p = Av * Wp * ih2;
     const double hev_L = Av * WL * ih2;
@@ -174,8 +188,10 @@ EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr,
 
     const double heff = heven + hodd;
     const double nu = J.nu, M = J.M;
-    const double s = sqrt(1.0 + 2.0 * nu * (heff - 1.0));
-    const double f = M / s;
+    const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
+    const double rs = eob_rsqrt(s2);
+    const double s = s2 * rs;
+    const double f = M * rs;
     HamPart o;
     o.H = M * s / nu;
     o.Hreal = M * s;

@@ -62,8 +62,9 @@ void phys_rhs(const double *st, const double *add, int n, double *k)
     }
 }
 
-// flux three ways: specialised per-mode code, the generic lane-group mode
-// evaluator, and the same with the lane-group shared pieces
+// flux four ways: specialised per-mode code, the generic lane-group mode
+// evaluator, the same with the lane-group shared pieces (out[3i .. 3i+2]),
+// and the evaluator of groups of 8 or more lanes (out[3n + i])
 void phys_flux_both(const double *st, const double *add, int n, double *out)
 {
     for (int i = 0; i < n; ++i) {
@@ -101,6 +102,8 @@ void phys_flux_both(const double *st, const double *add, int n, double *out)
         double sum2 = 0.0;
         for (int j = 0; j < 35; ++j) sum2 += eob::flux_mode_generic<10>(t, j, s2, e.Hreal * omega);
         out[3 * i + 2] = sum2 * omega * omega / (8.0 * eob::kPi);
+        // lanes of 8 or more: m factors computed per m, table Gamma products
+        out[3 * n + i] = eob::flux_eval_lanes(t, st[3 * n + i], omega, e.Hreal, e.omega_c);
     }
 }
 

