@@ -226,13 +226,17 @@ def config_block(cfg, args, extra=None):
 def census(args):
     """Every lane integrates the same binary, so the launch's lane-RHS count is
     exact; run under ncu with -k regex:k_integrate -s 3 -c 1 and divide the
-    FP64 instruction census by rhs_all_lanes."""
+    FP64 instruction census by rhs_all_lanes.  One lane per binary unless
+    --lanes is given."""
     import torch
     from eobgpu_gb300.pipeline import WaveformLikelihood
     cfg = workload.CONFIGS[1]
     p = workload.draw_params(cfg, batch=1, stream=0)
     P = torch.tensor(np.repeat(p, 128, axis=0), device="cuda")
-    wl = WaveformLikelihood(128, 4000, [(2, 2)], cfg.n_samples)
+    from eobgpu_gb300 import _lib
+    opt = _lib.default_options()
+    opt.lanes_per_binary = args.lanes or 1
+    wl = WaveformLikelihood(128, 4000, [(2, 2)], cfg.n_samples, options=opt)
     for _ in range(4):
         wl.prepare(P, cfg.dt, stages=3)
     torch.cuda.synchronize()
@@ -302,6 +306,8 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--fp64", action="store_true", help="configuration 3 in FP64 instead of mixed precision")
     ap.add_argument("--requests", type=int, default=2000, help="configuration 4: requests in the trace")
+    ap.add_argument("--no-graph", action="store_true", help="launch the path eagerly instead of replaying a CUDA graph")
+    ap.add_argument("--autotune", action="store_true", help="pick lanes per binary, block and spline tile by timing")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--max-steps", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=96)
@@ -347,6 +353,7 @@ def main():
     order = longest_first(P)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     chunked = None
+    tuned = None
     if args.config == 5:
         from eobgpu_gb300.pipeline import ChunkedLikelihood
         chunked = ChunkedLikelihood(B, cfg.n_samples, list(cfg.modes), args.max_steps, slots=2, options=opt,
@@ -356,10 +363,25 @@ def main():
         def run_any(Pd, Od):
             return chunked.run(Pd, D, cfg.dt, amp)
     else:
+        tuned = None
+        if args.autotune:
+            from eobgpu_gb300 import autotune
+            tuned = autotune.tune(P, D, cfg.dt, amp, list(cfg.modes), args.max_steps, base=opt)
+            opt = tuned.options(opt)
         wl = WaveformLikelihood(B, args.max_steps, list(cfg.modes), cfg.n_samples, device=device, options=opt)
+        if args.no_graph:
+            def run_any(Pd, Od):
+                return wl.run(Pd, D, cfg.dt, amp, order=Od)
+        else:
+            # the whole path as one CUDA graph; a step copies its parameters
+            # into the captured input and replays
+            Pg = P.clone()
+            graph = wl.capture(Pg, D, cfg.dt, amp)
 
-        def run_any(Pd, Od):
-            return wl.run(Pd, D, cfg.dt, amp, order=Od)
+            def run_any(Pd, Od):
+                if Pd is not Pg:
+                    Pg.copy_(Pd, non_blocking=True)
+                return graph.replay()
 
     def step():
         return run_any(P, order)
@@ -391,9 +413,13 @@ def main():
         for i in range(args.steps):
             flush.fill_(float(i))
             ev2[i][0].record()
-            Pd = params_h.to(device, non_blocking=True)
-            Od = order_h.to(device, non_blocking=True)
-            l_d, s_d = run_any(Pd, Od)
+            if chunked is None and not args.no_graph:
+                Pg.copy_(params_h, non_blocking=True)
+                l_d, s_d = graph.replay()
+            else:
+                Pd = params_h.to(device, non_blocking=True)
+                Od = order_h.to(device, non_blocking=True)
+                l_d, s_d = run_any(Pd, Od)
             lnl_h.copy_(l_d, non_blocking=True)
             st_h.copy_(s_d, non_blocking=True)
             ev2[i][1].record()
@@ -457,6 +483,13 @@ def main():
                 "work": f"{F_RHS:.0f} FP64 FLOP per RHS x {cnt['rhs_binaries']} RHS evaluations",
                 "lane_occupancy": cnt["rhs_binaries"] / max(1, cnt["rhs_all_lanes"])}
 
+    graphed = chunked is None and not args.no_graph
+    extra_cfg = {"cuda_graph": graphed}
+    if chunked is not None:
+        extra_cfg["chunks"] = chunked.info(B)
+    if chunked is None and tuned is not None:
+        extra_cfg["autotune"] = {"lanes_per_binary": tuned.lanes_per_binary, "block": tuned.block,
+                                 "spline_series_per_block": tuned.spline_series_per_block, "table": tuned.table}
     line = None
     if rank == 0:
         cpu_base = None
@@ -472,8 +505,9 @@ def main():
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64 integrator; f64 phase + f32 amplitude/sincos/residual synthesis" if mixed else "f64",
                 "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
-                "config": config_block(cfg, args, extra=({"chunks": chunked.info(B)} if chunked else None)),
-                "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": int(B * 5 * 8 + B * 4),
+                "config": config_block(cfg, args, extra=extra_cfg),
+                "e2e": {"value": e2e_value, "unit": "evals/s",
+                        "h2d_bytes_per_step": int(B * 5 * 8 + (0 if graphed else B * 4)),
                         "d2h_bytes_per_step": int(B * 8 + B * 4)},
                 "roofline": roof, "cpu_baseline": cpu_base, "clocks": clocks,
                 "gpu_launches": launches_per_step * args.steps,

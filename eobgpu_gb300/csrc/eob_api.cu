@@ -21,7 +21,7 @@ void eob_options_default(eob_options *o)
     o->grid = 0;
     o->max_tries = 0;
     o->lanes_per_binary = 0;
-    o->pad_ = 0;
+    o->spline_tile = 0;
 }
 
 size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples)

@@ -6,9 +6,10 @@
 //  k_modes     one thread per packed trajectory row: h_lm e^{i m phi} for the
 //              requested modes (get_hlms, eob/seobnrv4phm.py:2138-2221, and
 //              the de-rotation of compute_full_waveform, :2331).
-//  k_spline    one thread per (binary, series): not-a-knot cubic spline with
-//              the reference's tridiagonal set-up and Thomas sweep
-//              (src/interpolate.cu:10-267).
+//  k_spline    one warp per (binary, series): not-a-knot cubic spline with
+//              the reference's tridiagonal set-up (src/interpolate.cu:10-267),
+//              solved by a partition method (a block of rows per lane, the
+//              block boundaries by lane 0) instead of one serial sweep.
 //  k_synth     one block per 1024-sample chunk of one binary: spline
 //              evaluation on the uniform grid (eob/seobnrv4phm.py:274-386,
 //              2310-2372), mode sum (BBHWaveformTD, :715-721) and the
@@ -218,27 +219,190 @@ __device__ void spline_one(const double *x, const double *y, int n, double *Bv, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_spline(Ws w, int B, int nsubs, int mixed)
+// Row i of the not-a-knot slope system (src/interpolate.cu:10-120):
+// a x_{i-1} + b x_i + c x_{i+1} = d.
+__device__ __forceinline__ void spline_row(const double *x, const double *y, int n, int i, double *a, double *b,
+                                           double *c, double *d)
 {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int i0, i1, i2;
+    if (i == n - 1) { i0 = n - 3; i1 = n - 2; i2 = n - 1; }
+    else if (i == 0) { i0 = 0; i1 = 1; i2 = 2; }
+    else { i0 = i - 1; i1 = i; i2 = i + 1; }
+    const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
+    const double dx1 = x1 - x0, dx2 = x2 - x1, dd = x2 - x0;
+    const double y1 = y[i1];
+    const double s1 = (y1 - y[i0]) / dx1, s2 = (y[i2] - y1) / dx2;
+    if (i == n - 1) {
+        *d = (dx2 * dx2 * s1 + (2 * dd + dx2) * dx1 * s2) / dd;
+        *b = dx1; *a = dd; *c = 0.0;
+    } else if (i == 0) {
+        *d = ((dx1 + 2 * dd) * dx2 * s1 + dx1 * dx1 * s2) / dd;
+        *c = dd; *a = 0.0; *b = dx2;
+    } else {
+        *d = 3.0 * (dx2 * s1 + dx1 * s2);
+        *b = 2 * (dx1 + dx2); *c = dx1; *a = dx2;
+    }
+}
+
+constexpr int kSplineRowsPerLane = 8;  // partition the system only when every lane gets this many rows
+constexpr int kSplineMaxTile = 8;      // series (warps) per block
+
+// One warp per series (binary, sub).  The tridiagonal slope system is solved
+// by a partition method: lane k owns a contiguous block of rows, eliminates it
+// with three right-hand sides (the data and the two couplings to the
+// neighbouring blocks), lane 0 solves the 2x2-block tridiagonal system of the
+// block boundaries (gathered by shuffles), and every lane back-substitutes
+// its rows; the cubic coefficients are then computed lane-strided.  Scratch:
+// the series' own coefficient rows (ld/dg/ud/Bv = c3/c2/c1/rhs arrays).
+__global__ void __launch_bounds__(32 * kSplineMaxTile) k_spline(Ws w, int B, int nsubs, int mixed)
+{
+    __shared__ double s_z[kSplineMaxTile][2][32];   // boundary solution: u_j = x_{e_j}, t_{j+1} = x_{s_{j+1}}
+    __shared__ double s_f[kSplineMaxTile][5][32];   // reduced elimination per interface: d01, d10, f0, f1, ws_{j+1}
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * (blockDim.x >> 5) + wib;  // uniform across the warp
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.queue[6] = (unsigned long long)mixed;
     if (idx >= B * nsubs) return;
-    if (idx == 0) w.queue[6] = (unsigned long long)mixed;
     const int b = idx / nsubs, sub = idx % nsubs;
     if (w.npts[b] <= 0) return;
     const int n = w.nsteps[b];
     const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
     const size_t base = (size_t)w.row_off[b];
     const size_t o = (size_t)sub * Rc + base;
-    spline_one(w.tin + base, w.ys + o, n, w.cD + o, w.cA + o, w.cB + o, w.cC + o);
+    const double *x = w.tin + base, *y = w.ys + o;
+    double *Bv = w.cD + o, *ud = w.cA + o, *dg = w.cB + o, *ld = w.cC + o;
+
+    for (int i = lane; i < n; i += 32) spline_row(x, y, n, i, &ld[i], &dg[i], &ud[i], &Bv[i]);
+    __syncwarp();
+
+    int P = n / kSplineRowsPerLane;
+    if (P > 32) P = 32;
+    if (P < 2) {
+        if (lane == 0) {  // short series: one Thomas sweep
+            for (int i = 1; i < n; ++i) {
+                const double wgt = ld[i] / dg[i - 1];
+                dg[i] = dg[i] - wgt * ud[i - 1];
+                Bv[i] = Bv[i] - wgt * Bv[i - 1];
+            }
+            Bv[n - 1] = Bv[n - 1] / dg[n - 1];
+            for (int i = n - 2; i >= 0; --i) Bv[i] = (Bv[i] - ud[i] * Bv[i + 1]) / dg[i];
+        }
+    } else {
+        const int q = n / P, r = n % P;
+        const bool own = lane < P;
+        const int s0 = lane * q + min(lane, r);
+        const int e0 = s0 + q + (lane < r ? 1 : 0) - 1;
+        double gs = 0.0, vs = 0.0, ws = 0.0, ge = 0.0, ve = 0.0, we = 0.0;
+        if (own) {
+            // forward elimination; dg <- 1/b', Bv <- d', ld <- v' (v' starts as a_s e_1)
+            double ib = 1.0 / dg[s0], dp = Bv[s0], vp = ld[s0];
+            dg[s0] = ib;
+            ld[s0] = vp;
+            for (int i = s0 + 1; i <= e0; ++i) {
+                const double wgt = ld[i] * ib;
+                ib = 1.0 / (dg[i] - wgt * ud[i - 1]);
+                dp = Bv[i] - wgt * dp;
+                vp = -wgt * vp;
+                dg[i] = ib;
+                Bv[i] = dp;
+                ld[i] = vp;
+            }
+            // back substitution of g (data), v (left coupling), w (right coupling, c_e at row e only)
+            double gx = dp * ib, vx = vp * ib, wx = ud[e0] * ib;
+            Bv[e0] = gx;
+            ld[e0] = vx;
+            dg[e0] = wx;
+            ge = gx;
+            ve = vx;
+            we = wx;
+            for (int i = e0 - 1; i >= s0; --i) {
+                const double ibi = dg[i], ci = ud[i];
+                gx = (Bv[i] - ci * gx) * ibi;
+                vx = (ld[i] - ci * vx) * ibi;
+                wx = -ci * wx * ibi;
+                Bv[i] = gx;
+                ld[i] = vx;
+                dg[i] = wx;
+            }
+            gs = gx;
+            vs = vx;
+            ws = wx;
+        }
+        // reduced system over the P-1 block interfaces j (between blocks j, j+1),
+        // unknowns Z_j = (u_j, t_{j+1}) = (x at the end of block j, x at the start of block j+1):
+        //   u_j + ve_j u_{j-1} + we_j t_{j+1} = ge_j
+        //   vs_{j+1} u_j + t_{j+1} + ws_{j+1} t_{j+2} = gs_{j+1}
+        // a 2x2-block tridiagonal system, eliminated by lane 0 (gathers by shuffles)
+        double k00 = 0.0, k01 = 0.0, f0 = 0.0, f1 = 0.0;
+        for (int j = 0; j < P - 1; ++j) {
+            const double vej = __shfl_sync(0xffffffffu, ve, j), wej = __shfl_sync(0xffffffffu, we, j);
+            const double gej = __shfl_sync(0xffffffffu, ge, j), wsj = __shfl_sync(0xffffffffu, ws, j);
+            const double vsn = __shfl_sync(0xffffffffu, vs, j + 1), wsn = __shfl_sync(0xffffffffu, ws, j + 1);
+            const double gsn = __shfl_sync(0xffffffffu, gs, j + 1);
+            if (lane == 0) {
+                double d01 = wej, h0 = gej;
+                if (j > 0) {
+                    d01 -= vej * k01 * wsj;
+                    h0 -= vej * (k00 * f0 + k01 * f1);
+                }
+                const double idet = 1.0 / (1.0 - d01 * vsn);
+                k00 = idet;
+                k01 = -d01 * idet;
+                f0 = h0;
+                f1 = gsn;
+                s_f[wib][0][j] = d01;
+                s_f[wib][1][j] = vsn;
+                s_f[wib][2][j] = h0;
+                s_f[wib][3][j] = gsn;
+                s_f[wib][4][j] = wsn;
+            }
+        }
+        if (lane == 0) {
+            double tn = 0.0;  // t_{j+2} of the interface after j
+            for (int j = P - 2; j >= 0; --j) {
+                const double d01 = s_f[wib][0][j], d10 = s_f[wib][1][j];
+                const double h0 = s_f[wib][2][j];
+                const double h1 = s_f[wib][3][j] - s_f[wib][4][j] * tn;
+                const double idet = 1.0 / (1.0 - d01 * d10);
+                const double uj = (h0 - d01 * h1) * idet;
+                const double tj = (h1 - d10 * h0) * idet;
+                s_z[wib][0][j] = uj;
+                s_z[wib][1][j] = tj;
+                tn = tj;
+            }
+        }
+        __syncwarp();
+        if (own) {
+            const double L = (lane > 0) ? s_z[wib][0][lane - 1] : 0.0;
+            const double R = (lane < P - 1) ? s_z[wib][1][lane] : 0.0;
+            for (int i = s0; i <= e0; ++i) Bv[i] = Bv[i] - ld[i] * L - dg[i] * R;
+        }
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+        if (i == n - 1) {
+            ud[i] = 0.0;
+            dg[i] = 0.0;
+            ld[i] = 0.0;
+            continue;
+        }
+        const double dx = x[i + 1] - x[i];
+        const double slope = (y[i + 1] - y[i]) / dx;
+        const double bi = Bv[i];
+        const double t = (bi + Bv[i + 1] - 2 * slope) / dx;
+        ud[i] = bi;
+        dg[i] = (slope - bi) / dx - t;
+        ld[i] = t / dx;
+    }
     if (mixed && sub >= 1) {
+        __syncwarp();
         // FP32 copies of the amplitude series for the mixed-precision synthesis
         const size_t S = (size_t)2 * w.L.Kc * Rc;
         float *f = w.f32 + (size_t)(sub - 1) * Rc + base;
-        for (int i = 0; i < n; ++i) {
-            f[i] = (float)w.ys[o + i];
-            f[S + i] = (float)w.cA[o + i];
-            f[2 * S + i] = (float)w.cB[o + i];
-            f[3 * S + i] = (float)w.cC[o + i];
+        for (int i = lane; i < n; i += 32) {
+            f[i] = (float)y[i];
+            f[S + i] = (float)ud[i];
+            f[2 * S + i] = (float)dg[i];
+            f[3 * S + i] = (float)ld[i];
         }
     }
 }
@@ -433,7 +597,9 @@ cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s)
     for (int j = 0; j < kMaxModes; ++j) { ma.ells[j] = a.ells[j]; ma.mms[j] = a.mms[j]; }
     k_modes<<<nsm * 8, 128, 0, s>>>(w, a.B, ma);
     const int nsubs = 1 + 2 * a.K;
-    k_spline<<<(a.B * nsubs + 127) / 128, 128, 0, s>>>(w, a.B, nsubs, a.opt.precision == 1 ? 1 : 0);
+    const int tile = (a.opt.spline_tile >= 1 && a.opt.spline_tile <= kSplineMaxTile) ? a.opt.spline_tile : 4;
+    const long long series = (long long)a.B * nsubs;
+    k_spline<<<(unsigned)((series + tile - 1) / tile), 32 * tile, 0, s>>>(w, a.B, nsubs, a.opt.precision == 1 ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -74,6 +74,10 @@ class WaveformLikelihood:
         self.mms = (ctypes.c_int * 5)(*[m for _, m in self.modes])
         self.last_B = 0
 
+    def capture(self, params: torch.Tensor, data: torch.Tensor, dt: float, amp: float) -> "CapturedLikelihood":
+        """The fused lnL path on these (static) tensors as a replayable CUDA graph."""
+        return CapturedLikelihood(self, params, data, dt, amp)
+
     def set_modes(self, modes):
         """Modes of the following calls (at most max_modes of them)."""
         modes = [tuple(int(v) for v in m) for m in modes]
@@ -218,6 +222,46 @@ class WaveformLikelihood:
         traj = self._dev_array(v.traj, self.last_B * self.max_steps * 5, torch.float64).view(-1, self.max_steps, 5)
         first = traj[:, 0].cpu().numpy()
         return np.stack([first[:, 1], first[:, 4], first[:, 3]], axis=1)
+
+
+class CapturedLikelihood:
+    """One WaveformLikelihood.run captured as a CUDA graph.
+
+    The graph holds the whole path (setup, persistent integrator, packing,
+    multipoles, splines, synthesis + lnL: about ten launches and one memset)
+    for fixed input tensors; a new batch is copied into `params` (and, if it
+    changes, `data`) in place and `replay()` re-runs every launch at the cost
+    of one graph launch.  The batch size, modes and options are those of the
+    capture; `order` (queue order) is recomputed from `params` inside the
+    graph."""
+
+    def __init__(self, wl: "WaveformLikelihood", params: torch.Tensor, data: torch.Tensor, dt: float, amp: float):
+        self.wl = wl
+        self.params = params
+        self.data = data
+        self.B = int(params.shape[0])
+        self.lnl = torch.empty(self.B, dtype=torch.float64, device=wl.device)
+        self.status = torch.empty(self.B, dtype=torch.int32, device=wl.device)
+        self.order = torch.empty(self.B, dtype=torch.int32, device=wl.device)
+        self.graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(wl.device)
+        side.wait_stream(torch.cuda.current_stream(wl.device))
+        with torch.cuda.stream(side):  # warm-up outside the capture
+            self._body(dt, amp, side)
+        torch.cuda.current_stream(wl.device).wait_stream(side)
+        with torch.cuda.graph(self.graph):
+            self._body(dt, amp, torch.cuda.current_stream(wl.device))
+
+    def _body(self, dt, amp, stream):
+        self.order.copy_(longest_first(self.params))
+        self.wl.run(self.params, self.data, dt, amp, order=self.order, lnl=self.lnl, status=self.status,
+                    stream=stream)
+
+    def replay(self):
+        """Re-run the captured path on the current contents of params/data;
+        returns the (static) lnl and status tensors."""
+        self.graph.replay()
+        return self.lnl, self.status
 
 
 def chunk_size_for_budget(budget_bytes: int, max_steps: int, n_modes: int, n_samples: int, upper: int) -> int:

@@ -49,7 +49,7 @@ typedef struct eob_options {
     int grid;               /* integrator blocks (0 = one wave of resident blocks) */
     long long max_tries;    /* step attempts per pass before giving up (0 = 2 * max_steps + 100) */
     int lanes_per_binary;   /* integrator lanes per binary: 1, 2, 4, 8, 16, 32 (0 = chosen from the batch size) */
-    int pad_;
+    int spline_tile;        /* spline build: series (one warp each) per block, 1..8 (0 = default 4) */
 } eob_options;
 
 void eob_options_default(eob_options *o);

@@ -78,6 +78,32 @@ def test_config1_strain_vs_reference(cfg1_run, torch_cuda):
         assert abs(dphi) < 1e-5, dphi
 
 
+def test_config1_splines_vs_oracle(cfg1_run, oracle, torch_cuda):
+    """The warp-partitioned spline build against the oracle's serial sweep on
+    the same knots (phase and the two amplitude series of every binary)."""
+    torch = torch_cuda
+    wl, lnl, st, c = cfg1_run
+    v = wl.views()
+    B = wl.last_B
+    nsteps = wl._dev_array(v.nsteps, B, torch.int32).cpu().numpy()
+    roff = wl._dev_array(v.row_off, B, torch.int64).cpu().numpy()
+    Rc = int(v.rows_capacity)
+    tin = wl._dev_array(v.tin, Rc, torch.float64).cpu().numpy()
+    arrs = [wl._dev_array(a, v.nsubs * Rc, torch.float64).cpu().numpy()
+            for a in (v.spline_y, v.spline_c1, v.spline_c2, v.spline_c3)]
+    for b in range(B):
+        n = int(nsteps[b])
+        o = int(roff[b])
+        x = tin[o:o + n]
+        for sub in range(v.nsubs):
+            y = arrs[0][sub * Rc + o: sub * Rc + o + n]
+            c1, c2, c3 = oracle.interpolate_td(x, y, [n], 1, 1)
+            for got, ref in zip(arrs[1:], (c1, c2, c3)):
+                g = got[sub * Rc + o: sub * Rc + o + n - 1]
+                r = ref[:n - 1]
+                assert np.max(np.abs(g - r)) <= 1e-10 * np.max(np.abs(r)), (b, sub)
+
+
 def test_config1_lnl_vs_reference(cfg1_run):
     _, lnl, _, c = cfg1_run
     rel = np.abs(lnl / c["lnl"] - 1)
@@ -108,3 +134,33 @@ def test_config1_lanes_per_binary(torch_cuda, golden, G):
     assert np.all(np.abs(lnl / c["lnl"] - 1) < 1e-9), (G, lnl / c["lnl"] - 1)
     nsteps, npts, _, _ = wl.trajectories()
     np.testing.assert_array_equal(nsteps, c["nsteps"])
+
+
+def test_config1_rtol_1e10_vs_oracle(torch_cuda, golden, oracle):
+    """Configuration 1 as its benchmark states it, DOPR853 at rtol = atol =
+    1e-10 (the reference hard-codes 1e-12), against the oracle at the same
+    tolerances."""
+    torch = torch_cuda
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    c = golden["config1"]
+    opt = _lib.default_options()
+    opt.rtol = opt.atol = 1e-10
+    P = torch.tensor(c["params"], dtype=torch.float64, device="cuda")
+    d = torch.tensor(c["data"], dtype=torch.float64, device="cuda")
+    wl = WaveformLikelihood(len(P), 20000, [(2, 2)], int(c["N"]), options=opt)
+    lnl, st = wl.run(P, d, float(c["dt"]), float(c["amp"]))
+    nsteps = wl.trajectories()[0]
+    lnl = lnl.cpu().numpy()
+    assert np.all(st.cpu().numpy() == 0)
+    same = 0
+    for b in range(len(P)):
+        r = oracle.lnl_one(c["params"][b], float(c["dt"]), int(c["N"]), [(2, 2)], c["data"], float(c["amp"]),
+                           rtol=1e-10, atol=1e-10)
+        assert r["status"] == 0
+        if r["nsteps"] == nsteps[b]:
+            same += 1
+            assert abs(lnl[b] / r["lnl"] - 1) < 1e-9, b
+        else:
+            assert abs(lnl[b] / r["lnl"] - 1) < 1e-6, b
+    assert same >= len(P) // 2
