@@ -91,6 +91,23 @@ __device__ __forceinline__ double pow4(double x)
     return x2 * x2;
 }
 
+// weights of stage s (2..12) in the three running sums (zero where a stage
+// does not enter); selects on compile-time constants, no table lookups
+__device__ __forceinline__ void stage_weights(int s, double *wb, double *we, double *wh)
+{
+    double b = 0.0, e = 0.0, hh = 0.0;
+    b = (s == 6) ? dp::b6 : b;     e = (s == 6) ? dp::er6 : e;
+    b = (s == 7) ? dp::b7 : b;     e = (s == 7) ? dp::er7 : e;
+    b = (s == 8) ? dp::b8 : b;     e = (s == 8) ? dp::er8 : e;
+    b = (s == 9) ? dp::b9 : b;     e = (s == 9) ? dp::er9 : e;     hh = (s == 9) ? -dp::bhh2 : hh;
+    b = (s == 10) ? dp::b10 : b;   e = (s == 10) ? dp::er10 : e;
+    b = (s == 11) ? dp::b11 : b;   e = (s == 11) ? dp::er11 : e;
+    b = (s == 12) ? dp::b12 : b;   e = (s == 12) ? dp::er12 : e;   hh = (s == 12) ? -dp::bhh3 : hh;
+    *wb = b;
+    *we = e;
+    *wh = hh;
+}
+
 // Lane state
 enum Phase : int { kIdle = 0, kStartPass = 1, kStage = 2, kStopTest = 3 };
 
@@ -120,7 +137,13 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - sub));
     // per-lane DOPR853 state
     double k[11][4];  // slopes k1..k10 (slot 0 unused)
-    double y[4], ynew[4], arg[4];
+    double y[4], arg[4];
+    // running sums over the stages of the current attempt: the 8th-order
+    // increment sum b_s k_s, the 5th-order error sum er_s k_s and the 3rd-order
+    // correction -bhh_s k_s; each stage adds its own term as soon as its slope
+    // exists, so the end of a step is short (lanes of one warp reach it at
+    // different iterations, and that code runs for the whole warp)
+    double acc_b[4], acc_e[4], acc_h[4];
     double x = 0.0, h = 0.0, hfix = 0.0, errOld = 1e-4;
     double om_hist[4] = {0.0, 0.0, 0.0, 0.0};  // omega of rows (step-4 .. step-1) % 4
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
@@ -195,7 +218,12 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
 
         // ------------------------------------------------ advance the lane
         if (phase == kStartPass) {
-            for (int q = 0; q < 4; ++q) k[1][q] = kk[q];
+            for (int q = 0; q < 4; ++q) {
+                k[1][q] = kk[q];
+                acc_b[q] = dp::b1 * kk[q];
+                acc_e[q] = dp::er1 * kk[q];
+                acc_h[q] = -dp::bhh1 * kk[q];
+            }
             errOld = 1e-4;
             prevReject = false;
             tries = 0;
@@ -206,22 +234,27 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
             continue;
         }
         if (phase == kStage) {
-            for (int q = 0; q < 4; ++q) k[out_slot][q] = kk[q];
+            double wb, we, wh;
+            stage_weights(stage, &wb, &we, &wh);
+            for (int q = 0; q < 4; ++q) {
+                k[out_slot][q] = kk[q];
+                acc_b[q] = fma(wb, kk[q], acc_b[q]);
+                acc_e[q] = fma(we, kk[q], acc_e[q]);
+                acc_h[q] = fma(wh, kk[q], acc_h[q]);
+            }
             if (stage < 12) {
                 ++stage;
                 continue;
             }
-            // error estimate (src/DOPR853.cu:537-618)
-            double e1 = 0.0, e2 = 0.0;
+            // error estimate (src/DOPR853.cu:537-618) from the running sums
+            double e1 = 0.0, e2 = 0.0, ynew[4];
             for (int q = 0; q < 4; ++q) {
-                const double t = dp::b1 * k[1][q] + dp::b6 * k[6][q] + dp::b7 * k[7][q] + dp::b8 * k[8][q] +
-                                 dp::b9 * k[9][q] + dp::b10 * k[10][q] + dp::b11 * k[2][q] + dp::b12 * k[3][q];
+                const double t = acc_b[q];
                 ynew[q] = y[q] + h * t;
                 const double mx = (y[q] > ynew[q]) ? y[q] : ynew[q];
                 const double sk = 1.0 / (a.atol + a.rtol * mx);
-                e2 += pow4((t - dp::bhh1 * k[1][q] - dp::bhh2 * k[9][q] - dp::bhh3 * k[3][q]) * sk);
-                e1 += pow4((dp::er1 * k[1][q] + dp::er6 * k[6][q] + dp::er7 * k[7][q] + dp::er8 * k[8][q] +
-                            dp::er9 * k[9][q] + dp::er10 * k[10][q] + dp::er11 * k[2][q] + dp::er12 * k[3][q]) * sk);
+                e2 += pow4((t + acc_h[q]) * sk);
+                e1 += pow4(acc_e[q] * sk);
             }
             double denom = e1 + 0.01 * e2;
             denom = (denom < 0.0) ? 1.0 : denom;
@@ -277,6 +310,11 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 if (tries >= a.max_tries) { st |= EOB_ST_TRIES; end = true; }
                 if (!end) {
                     stage = 2;  // retry with the new h; k1 unchanged
+                    for (int q = 0; q < 4; ++q) {
+                        acc_b[q] = dp::b1 * k[1][q];
+                        acc_e[q] = dp::er1 * k[1][q];
+                        acc_h[q] = -dp::bhh1 * k[1][q];
+                    }
                     continue;
                 }
                 phase = -1;  // fall through to end-of-pass handling
@@ -287,7 +325,12 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         bool end_pass = false;
         if (phase == kStopTest) {
             // stopping rule on the accepted state (kk = f(y))
-            for (int q = 0; q < 4; ++q) k[1][q] = kk[q];
+            for (int q = 0; q < 4; ++q) {
+                k[1][q] = kk[q];
+                acc_b[q] = dp::b1 * kk[q];
+                acc_e[q] = dp::er1 * kk[q];
+                acc_h[q] = -dp::bhh1 * kk[q];
+            }
             const double r = y[0], drdt = kk[0], omega = kk[1], dprdt = kk[2];
             int code = 0;
             if (r < 1.0) code = 2;

@@ -65,3 +65,33 @@ def test_mixed_requires_mixed_spline_build(env):
     wl.options.precision = 1
     lnl, st = wl.synth_lnl(4, torch.tensor(data, device="cuda"), cfg.dt, amp)
     assert np.all(np.isnan(lnl.cpu().numpy()))
+
+
+def test_mixed_vs_oracle(env, oracle):
+    """Mixed precision against the FP64 oracle on a sample of the batch:
+    mismatch <= 1e-6, |dlnL| <= 1e-3, phase at the amplitude peak within
+    1e-5 rad.  The worst values are written to $EOB_ACCURACY_OUT if set."""
+    import json
+    import os
+    torch, cfg, params, data, amp, N = env
+    lmx, smx, hmx = _run(torch, cfg, params, data, amp, N, 1)
+    worst = {"max_dphi_rad": 0.0, "max_mismatch": 0.0, "max_abs_dlnl": 0.0, "sample": 0}
+    for b in range(0, len(params), 8):
+        r = oracle.lnl_one(params[b], cfg.dt, N, MODES, data, amp, max_step=6000, want_detail=True)
+        assert r["status"] == 0
+        a, c = r["h"], hmx[b]
+        ov = np.real(np.vdot(a, c)) / np.sqrt(np.real(np.vdot(a, a)) * np.real(np.vdot(c, c)))
+        k = int(np.argmax(np.abs(a)))
+        dphi = abs((np.angle(c[k]) - np.angle(a[k]) + np.pi) % (2 * np.pi) - np.pi)
+        dl = abs(lmx[b] - r["lnl"])
+        worst["max_dphi_rad"] = max(worst["max_dphi_rad"], float(dphi))
+        worst["max_mismatch"] = max(worst["max_mismatch"], float(1 - ov))
+        worst["max_abs_dlnl"] = max(worst["max_abs_dlnl"], float(dl))
+        worst["sample"] += 1
+        assert 1 - ov <= 1e-6, (b, 1 - ov)
+        assert dl <= 1e-3, (b, dl)
+        assert dphi <= 1e-5, (b, dphi)
+    out = os.environ.get("EOB_ACCURACY_OUT")
+    if out:
+        with open(out, "w") as f:
+            json.dump({"config": "3 (mixed precision, 5 modes, N=2^15 sample)", **worst}, f)
