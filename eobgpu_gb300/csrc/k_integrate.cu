@@ -410,6 +410,13 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
 template <int G>
 cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
 {
+    // no shared memory: give the SM's unified L1/shared storage to L1, where
+    // the lanes' coefficient tables and slope arrays live
+    static bool carveout_set = false;
+    if (!carveout_set) {
+        cudaFuncSetAttribute(k_integrate<G>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        carveout_set = true;
+    }
     if (grid <= 0) {
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
