@@ -298,8 +298,9 @@ def run_serving(args, ws, rank, local):
     torch.cuda.set_device(device)
     _, data, amp = make_inputs(cfg, rank, device, args.max_steps)
     lanes = args.lanes or 8
-    server = LikelihoodServer(data, cfg.dt, amp, max_batch=1024, max_steps=args.max_steps, slots=2,
-                              lanes_per_binary=lanes, device=device)
+    classes = [(1500, 1024, 2), (args.max_steps, 512, 1)]
+    server = LikelihoodServer(data, cfg.dt, amp, classes=classes, lanes_per_binary=lanes,
+                              precision=0 if args.fp64 else 1, device=device)
     trace = workload.serving_trace(args.requests, 1.0, stream=rank)
     for _ in range(args.warmup):
         server.evaluate(trace.params[0])
@@ -318,11 +319,14 @@ def run_serving(args, ws, rank, local):
         value = nbin / wall
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.fp64 else "f64 integrator; f64 phase + f32 amplitude/sincos/residual synthesis",
                 "data": "synthetic: seeded Poisson trace of walker requests, white noise + one injection at SNR 30",
-                "config": {"workload": "config 4: serving, continuous batching over 2 concurrent slots",
+                "config": {"workload": "config 4: serving, continuous batching over concurrent slots",
                            "requests": args.requests, "request_size": [1, 512], "rate_hz": rate,
-                           "target_busy": 0.7, "max_batch": 1024, "slots": 2, "lanes_per_binary": lanes,
+                           "target_busy": 0.7, "classes_max_steps_batch_slots": classes,
+                           "admission": "by estimated trajectory rows (chirp-time fit x3), re-run on overflow",
+                           "requeued": int(sum(r["requeued"] for r in results)), "lanes_per_binary": lanes,
                            "max_steps": args.max_steps, "dt_s": cfg.dt, "n_samples": cfg.n_samples,
                            "l2": "inputs of each batch are new; no flush (latency run)"},
                 "e2e": {"value": value, "unit": "evals/s",

@@ -46,3 +46,21 @@ def test_trace_replay(server):
     assert np.all(res["latency_s"] > 0)
     assert res["p99_ms"] >= res["p50_ms"] > 0
     assert res["binaries"] == sum(len(r) for r in reqs)
+
+
+def test_classes_requeue_matches_single_class(server):
+    """Two trajectory-length classes with a deliberately short first class:
+    binaries that outgrow it (status MAXSTEP) are re-run in the second, and
+    every lnL equals the single-class server's bitwise."""
+    from eobgpu_gb300 import workload
+    from eobgpu_gb300.serving import LikelihoodServer
+    tr = workload.serving_trace(6, 1000.0, stream=6)
+    reqs = [p[:48] for p in tr.params]
+    ref = server.run_trace(np.zeros(len(reqs)), reqs)
+    cls = LikelihoodServer(server.data.cpu().numpy(), server.dt, server.amp, classes=[(350, 64, 1), (4000, 96, 1)],
+                           lanes_per_binary=8, row_safety=0.3)
+    res = cls.run_trace(np.zeros(len(reqs)), reqs)
+    assert res["requeued"] > 0
+    for a, b, s in zip(ref["lnl"], res["lnl"], res["status"]):
+        assert np.all(s == 0)
+        assert np.array_equal(a, b)
