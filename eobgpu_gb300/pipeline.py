@@ -285,30 +285,60 @@ class ChunkedLikelihood:
     (default: 60 % of the free device memory) for batches of up to
     max_batch binaries; a call orders its batch longest first, cuts it into
     chunks and alternates them over the slots' streams, so that a chunk
-    starts while the ragged tail of the previous one still runs."""
+    starts while the ragged tail of the previous one still runs.
+
+    head > 0 runs the `head` longest binaries of a call on their own
+    workspace and stream with head_lanes lanes per binary, concurrently with
+    the rest: the bulk of a large batch is throughput bound (one lane per
+    binary), but its few longest binaries would set the time of the first
+    chunk; with several lanes each, their sequential chains are shorter."""
 
     def __init__(self, max_batch: int, n_samples: int, modes=((2, 2),), max_steps: int = 16000,
                  hbm_budget_bytes: int | None = None, slots: int = 2, options: _lib.EobOptions | None = None,
-                 device="cuda"):
+                 head: int = 0, head_lanes: int = 8, device="cuda"):
         self.device = torch.device(device)
         if hbm_budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget_bytes = int(0.6 * free)
         self.budget = int(hbm_budget_bytes)
-        per_slot = self.budget // max(1, slots)
-        self.chunk = chunk_size_for_budget(per_slot, max_steps, len(modes), n_samples, max(1, -(-max_batch // slots)))
+        lib = _lib.load()
+        self.head = max(0, min(int(head), int(max_batch) - 1))
+        head_ws = int(lib.eob_workspace_bytes(self.head, max_steps, len(modes), n_samples)) if self.head else 0
+        per_slot = (self.budget - head_ws) // max(1, slots)
+        rest = int(max_batch) - self.head
+        self.chunk = chunk_size_for_budget(per_slot, max_steps, len(modes), n_samples, max(1, -(-rest // slots)))
         if self.chunk < 1:
             raise _lib.EOBError(f"HBM budget {self.budget} B admits no binary at max_steps={max_steps}, "
                                 f"N={n_samples}")
-        nslots = min(slots, -(-max_batch // self.chunk))
+        nslots = min(slots, -(-rest // self.chunk))
         self.engines = [WaveformLikelihood(self.chunk, max_steps, modes, n_samples, device=self.device,
                                            options=options) for _ in range(nslots)]
         self.streams = [torch.cuda.Stream(self.device) for _ in range(nslots)]
-        self.identity = torch.arange(self.chunk, dtype=torch.int32, device=self.device)
+        self.identity = torch.arange(max(self.chunk, self.head), dtype=torch.int32, device=self.device)
+        self.head_engine = None
+        if self.head:
+            ho = _lib.EobOptions.from_buffer_copy(options) if options is not None else _lib.default_options()
+            ho.lanes_per_binary = int(head_lanes)
+            self.head_lanes = int(head_lanes)
+            self.head_engine = WaveformLikelihood(self.head, max_steps, modes, n_samples, device=self.device,
+                                                  options=ho)
+            self.head_stream = torch.cuda.Stream(self.device)
 
     def info(self, B: int):
-        return {"chunk": self.chunk, "chunks": -(-B // self.chunk), "slots": len(self.engines),
-                "workspace_bytes_per_slot": self.engines[0].ws_bytes, "budget_bytes": self.budget}
+        d = {"chunk": self.chunk, "chunks": -(-(B - self.head) // self.chunk), "slots": len(self.engines),
+             "workspace_bytes_per_slot": self.engines[0].ws_bytes, "budget_bytes": self.budget}
+        if self.head:
+            d.update({"head": self.head, "head_lanes_per_binary": self.head_lanes})
+        return d
+
+    def _one(self, e, s, idx, params, data, dt, amp, lnl, status):
+        with torch.cuda.stream(s):
+            P = params[idx].contiguous()
+            l, st = e.run(P, data, dt, amp, order=self.identity[:len(idx)], stream=s)
+            lnl[idx] = l
+            status[idx] = st
+            for t in (P, l, st, idx):
+                t.record_stream(s)
 
     def run(self, params: torch.Tensor, data: torch.Tensor, dt: float, amp: float):
         B = int(params.shape[0])
@@ -316,28 +346,28 @@ class ChunkedLikelihood:
         lnl = torch.empty(B, dtype=torch.float64, device=self.device)
         status = torch.empty(B, dtype=torch.int32, device=self.device)
         main = torch.cuda.current_stream(self.device)
+        head = min(self.head, B)
+        used = []
+        if head:
+            self.head_stream.wait_stream(main)
+            self._one(self.head_engine, self.head_stream, order[:head], params, data, dt, amp, lnl, status)
+            used.append(self.head_stream)
         n = len(self.engines)
-        for j, lo in enumerate(range(0, B, self.chunk)):
+        for j, lo in enumerate(range(head, B, self.chunk)):
             e, s = self.engines[j % n], self.streams[j % n]
             s.wait_stream(main)
-            with torch.cuda.stream(s):
-                idx = order[lo:lo + self.chunk]
-                P = params[idx].contiguous()
-                l, st = e.run(P, data, dt, amp, order=self.identity[:len(idx)], stream=s)
-                lnl[idx] = l
-                status[idx] = st
-                for t in (P, l, st, idx):
-                    t.record_stream(s)
-        for s in self.streams:
+            self._one(e, s, order[lo:lo + self.chunk], params, data, dt, amp, lnl, status)
+            used.append(s)
+        for s in used:
             main.wait_stream(s)
         return lnl, status
 
 
 def lnl_chunked(params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, modes=((2, 2),),
                 max_steps: int = 16000, hbm_budget_bytes: int | None = None, slots: int = 2,
-                options: _lib.EobOptions | None = None, device="cuda"):
+                options: _lib.EobOptions | None = None, head: int = 0, head_lanes: int = 8, device="cuda"):
     """One-shot ChunkedLikelihood: (lnl, status, info) in the input order."""
     c = ChunkedLikelihood(int(params.shape[0]), int(data.shape[0]), modes, max_steps, hbm_budget_bytes, slots,
-                          options, device)
+                          options, head, head_lanes, device)
     lnl, status = c.run(params, data, dt, amp)
     return lnl, status, c.info(int(params.shape[0]))

@@ -31,3 +31,30 @@ def test_chunked_equals_single_launch():
     assert info["chunk"] == 7 and info["chunks"] == 4 and info["slots"] == 2
     assert np.all(st2.cpu().numpy() == 0)
     assert np.array_equal(lnl.cpu().numpy(), ref.cpu().numpy())
+
+
+def test_chunked_with_head_equals_single_launch():
+    """The longest binaries on their own concurrent workspace (same lanes per
+    binary here, so the results must not move)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from eobgpu_gb300 import _lib, workload
+    from eobgpu_gb300.pipeline import WaveformLikelihood, lnl_chunked
+    cfg = workload.CONFIGS[1]
+    params = workload.draw_params(cfg, batch=24, stream=8)
+    data = workload.rng(1, 7).standard_normal(cfg.n_samples)
+    opts = _lib.default_options()
+    opts.lanes_per_binary = 4
+    P = torch.tensor(params, device="cuda")
+    D = torch.tensor(data, device="cuda")
+    wl = WaveformLikelihood(24, 4000, [(2, 2)], cfg.n_samples, options=opts)
+    ref, _ = wl.run(P, D, cfg.dt, 1.0)
+    budget = 2 * _lib.load().eob_workspace_bytes(8, 4000, 1, cfg.n_samples) + \
+        _lib.load().eob_workspace_bytes(5, 4000, 1, cfg.n_samples)
+    lnl, st, info = lnl_chunked(P, D, cfg.dt, 1.0, max_steps=4000, hbm_budget_bytes=budget, slots=2, options=opts,
+                                head=5, head_lanes=4)
+    torch.cuda.synchronize()
+    assert info["head"] == 5 and info["chunk"] == 8
+    assert np.all(st.cpu().numpy() == 0)
+    assert np.array_equal(lnl.cpu().numpy(), ref.cpu().numpy())
