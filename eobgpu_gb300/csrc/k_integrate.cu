@@ -4,9 +4,11 @@
 // 424-778) and its ~90 synchronous launches per step (src/DOPR853.cu:357-798,
 // src/EOB.cu:3046-3145) with one launch for the whole batch:
 //
-//  * one thread per binary (GB300 issues one FP64 warp-instruction per 64
-//    cycles per SM sub-partition whatever the active mask, so every lane must
-//    carry its own binary);
+//  * one lane per binary for large batches, or G lanes per binary (lane
+//    groups) when the longest binary's chain sets the time: GB300 issues one
+//    FP64 warp-instruction per 64 cycles per SM sub-partition whatever the
+//    active mask, so every lane must carry a binary or a distinct piece of
+//    one binary's arithmetic;
 //  * a flat per-lane state machine: each pass through the main loop evaluates
 //    exactly one right-hand side on every lane, whether that lane is in stage
 //    s of a step, in the stopping test, or starting a new pass or binary --
@@ -125,25 +127,45 @@ struct IntArgs {
     long long max_tries;
 };
 
+// component q of a 4-vector held in registers (selects, no local memory)
+__device__ __forceinline__ double pick4(const double v[4], int q)
+{
+    return q == 0 ? v[0] : (q == 1 ? v[1] : (q == 2 ? v[2] : v[3]));
+}
+
 template <int G>
-__global__ void __launch_bounds__(256) k_integrate(IntArgs a)
+__device__ __forceinline__ void integrate_body(const IntArgs &a)
 {
     // G consecutive lanes carry one binary; every lane of the group keeps the
-    // same state (identical arithmetic), the flux multipoles are split over
-    // the group, and only the group leader writes results.
+    // same control state, the Hamiltonian jets and flux multipoles are split
+    // over the group, and only the group leader writes scalar results.
+    //
+    // Groups of 4 or more lanes also split the DOPR853 state: lane q (mod 4)
+    // of the group holds component q of y, of the slopes and of the running
+    // stage sums, so the stage arguments, the sums and the per-component
+    // part of the error norm cost one lane's arithmetic instead of four (on
+    // GB300 an FP64 instruction costs the same issue slot whatever the number
+    // of active lanes).  The components are gathered by shuffles where the
+    // right-hand side or the stopping rule needs all four; the error norm
+    // adds the four components in the reference's order, so every lane
+    // reaches the same accept/reject decision with the same bits.
+    constexpr bool kDist = (G >= 4);
+    constexpr int NC = kDist ? 1 : 4;  // state components held by one lane
     const int lane = threadIdx.x & 31;
     const int sub = lane & (G - 1);
+    const int cq = kDist ? (sub & 3) : 0;  // the component a distributing lane holds
     const bool leader = (sub == 0);
+    const bool writer = kDist ? (sub < 4) : leader;  // writes trajectory components
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - sub));
-    // per-lane DOPR853 state
-    double k[11][4];  // slopes k1..k10 (slot 0 unused)
-    double y[4], arg[4];
+    // per-lane DOPR853 state (components comp(c) = kDist ? cq : c)
+    double k[11][NC];  // slopes k1..k10 (slot 0 unused)
+    double y[NC], argl[NC];
     // running sums over the stages of the current attempt: the 8th-order
     // increment sum b_s k_s, the 5th-order error sum er_s k_s and the 3rd-order
     // correction -bhh_s k_s; each stage adds its own term as soon as its slope
     // exists, so the end of a step is short (lanes of one warp reach it at
     // different iterations, and that code runs for the whole warp)
-    double acc_b[4], acc_e[4], acc_h[4];
+    double acc_b[NC], acc_e[NC], acc_h[NC];
     double x = 0.0, h = 0.0, hfix = 0.0, errOld = 1e-4;
     double om_hist[4] = {0.0, 0.0, 0.0, 0.0};  // omega of rows (step-4 .. step-1) % 4
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
@@ -172,11 +194,10 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 step = 0;
                 n_bin = 0;
                 x = 0.0;
-                for (int q = 0; q < 4; ++q) y[q] = rec->y0[q];
-                if (leader) {
-                    tr[0] = 0.0;
-                    for (int q = 0; q < 4; ++q) tr[1 + q] = y[q];
-                }
+                for (int c = 0; c < NC; ++c) y[c] = rec->y0[kDist ? cq : c];
+                if (leader) tr[0] = 0.0;
+                if (writer)
+                    for (int c = 0; c < NC; ++c) tr[1 + (kDist ? cq : c)] = y[c];
                 h = a.h_init;
                 hfix = a.h_init;
                 fix = false;
@@ -194,20 +215,26 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         int out_slot = 1;
         if (phase == kStage) {
             const int nt = dp::kNTerms[stage];
-            for (int q = 0; q < 4; ++q) {
+            for (int c = 0; c < NC; ++c) {
                 double ak = 0.0;
-                for (int t = 0; t < nt; ++t) ak += dp::kStage[stage][t].a * k[dp::kStage[stage][t].slot][q];
-                arg[q] = y[q] + h * ak;
+                for (int t = 0; t < nt; ++t) ak += dp::kStage[stage][t].a * k[dp::kStage[stage][t].slot][c];
+                argl[c] = y[c] + h * ak;
             }
             out_slot = dp::kOutSlot[stage];
-        } else if (phase == kStopTest) {
-            for (int q = 0; q < 4; ++q) arg[q] = y[q];
-        } else if (phase == kStartPass) {
-            for (int q = 0; q < 4; ++q) arg[q] = y[q];
+        } else if (phase == kStopTest || phase == kStartPass) {
+            for (int c = 0; c < NC; ++c) argl[c] = y[c];
         } else {
             // idle lane: evaluate a harmless state of binary 0 (result unused)
             rec = &a.bins[0];
-            for (int q = 0; q < 4; ++q) arg[q] = rec->y0[q];
+            for (int c = 0; c < NC; ++c) argl[c] = rec->y0[kDist ? cq : c];
+        }
+        double arg[4];
+        if constexpr (kDist) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) arg[q] = __shfl_sync(0xffffffffu, argl[0], q, G);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) arg[q] = argl[q];
         }
 
         // ------------------------------------------------ the one RHS per loop
@@ -215,14 +242,18 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
         else eob_rhs_group<G>(rec->jets, rec->flux, arg, kk, sub);
         if (!active) continue;
+        double km[NC];  // this lane's components of the new slope
+        if constexpr (kDist) km[0] = pick4(kk, cq);
+        else
+            for (int c = 0; c < NC; ++c) km[c] = kk[c];
 
         // ------------------------------------------------ advance the lane
         if (phase == kStartPass) {
-            for (int q = 0; q < 4; ++q) {
-                k[1][q] = kk[q];
-                acc_b[q] = dp::b1 * kk[q];
-                acc_e[q] = dp::er1 * kk[q];
-                acc_h[q] = -dp::bhh1 * kk[q];
+            for (int c = 0; c < NC; ++c) {
+                k[1][c] = km[c];
+                acc_b[c] = dp::b1 * km[c];
+                acc_e[c] = dp::er1 * km[c];
+                acc_h[c] = -dp::bhh1 * km[c];
             }
             errOld = 1e-4;
             prevReject = false;
@@ -236,25 +267,37 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         if (phase == kStage) {
             double wb, we, wh;
             stage_weights(stage, &wb, &we, &wh);
-            for (int q = 0; q < 4; ++q) {
-                k[out_slot][q] = kk[q];
-                acc_b[q] = fma(wb, kk[q], acc_b[q]);
-                acc_e[q] = fma(we, kk[q], acc_e[q]);
-                acc_h[q] = fma(wh, kk[q], acc_h[q]);
+            for (int c = 0; c < NC; ++c) {
+                k[out_slot][c] = km[c];
+                acc_b[c] = fma(wb, km[c], acc_b[c]);
+                acc_e[c] = fma(we, km[c], acc_e[c]);
+                acc_h[c] = fma(wh, km[c], acc_h[c]);
             }
             if (stage < 12) {
                 ++stage;
                 continue;
             }
             // error estimate (src/DOPR853.cu:537-618) from the running sums
-            double e1 = 0.0, e2 = 0.0, ynew[4];
-            for (int q = 0; q < 4; ++q) {
-                const double t = acc_b[q];
-                ynew[q] = y[q] + h * t;
-                const double mx = (y[q] > ynew[q]) ? y[q] : ynew[q];
+            double e1 = 0.0, e2 = 0.0, ynew[NC];
+            for (int c = 0; c < NC; ++c) {
+                const double t = acc_b[c];
+                ynew[c] = y[c] + h * t;
+                const double mx = (y[c] > ynew[c]) ? y[c] : ynew[c];
                 const double sk = 1.0 / (a.atol + a.rtol * mx);
-                e2 += pow4((t + acc_h[q]) * sk);
-                e1 += pow4(acc_e[q] * sk);
+                e2 += pow4((t + acc_h[c]) * sk);
+                e1 += pow4(acc_e[c] * sk);
+            }
+            if constexpr (kDist) {
+                // the four components' terms summed in component order, as
+                // the reference's loop over the equations does
+                const double p1 = e1, p2 = e2;
+                e1 = __shfl_sync(gmask, p1, 0, G);
+                e2 = __shfl_sync(gmask, p2, 0, G);
+#pragma unroll
+                for (int q = 1; q < 4; ++q) {
+                    e1 += __shfl_sync(gmask, p1, q, G);
+                    e2 += __shfl_sync(gmask, p2, q, G);
+                }
             }
             double denom = e1 + 0.01 * e2;
             denom = (denom < 0.0) ? 1.0 : denom;
@@ -291,14 +334,13 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
             ++tries;
             const bool bad = !(err == err) || !(h == h) || h == 0.0;
             if (ok) {
-                for (int q = 0; q < 4; ++q) y[q] = ynew[q];
+                for (int c = 0; c < NC; ++c) y[c] = ynew[c];
                 x = x + hOld;
                 ++step;
-                if (leader) {
-                    double *row = tr + (size_t)step * kTrajStride;
-                    row[0] = x;
-                    for (int q = 0; q < 4; ++q) row[1 + q] = y[q];
-                }
+                double *row = tr + (size_t)step * kTrajStride;
+                if (leader) row[0] = x;
+                if (writer)
+                    for (int c = 0; c < NC; ++c) row[1 + (kDist ? cq : c)] = y[c];
                 phase = kStopTest;  // next RHS: f(y_new) for the stopping rule and the next k1
                 if (bad) st |= EOB_ST_NAN;
             } else {
@@ -310,10 +352,10 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 if (tries >= a.max_tries) { st |= EOB_ST_TRIES; end = true; }
                 if (!end) {
                     stage = 2;  // retry with the new h; k1 unchanged
-                    for (int q = 0; q < 4; ++q) {
-                        acc_b[q] = dp::b1 * k[1][q];
-                        acc_e[q] = dp::er1 * k[1][q];
-                        acc_h[q] = -dp::bhh1 * k[1][q];
+                    for (int c = 0; c < NC; ++c) {
+                        acc_b[c] = dp::b1 * k[1][c];
+                        acc_e[c] = dp::er1 * k[1][c];
+                        acc_h[c] = -dp::bhh1 * k[1][c];
                     }
                     continue;
                 }
@@ -325,13 +367,13 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
         bool end_pass = false;
         if (phase == kStopTest) {
             // stopping rule on the accepted state (kk = f(y))
-            for (int q = 0; q < 4; ++q) {
-                k[1][q] = kk[q];
-                acc_b[q] = dp::b1 * kk[q];
-                acc_e[q] = dp::er1 * kk[q];
-                acc_h[q] = -dp::bhh1 * kk[q];
+            for (int c = 0; c < NC; ++c) {
+                k[1][c] = km[c];
+                acc_b[c] = dp::b1 * km[c];
+                acc_e[c] = dp::er1 * km[c];
+                acc_h[c] = -dp::bhh1 * km[c];
             }
-            const double r = y[0], drdt = kk[0], omega = kk[1], dprdt = kk[2];
+            const double r = arg[0], drdt = kk[0], omega = kk[1], dprdt = kk[2];  // arg = y here
             int code = 0;
             if (r < 1.0) code = 2;
             else if (r < 6.0 && drdt > 0.0) code = 3;
@@ -372,6 +414,8 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
                 phase = kIdle;
                 continue;
             }
+            // the rows were written by other lanes of the group: make them visible
+            __syncwarp(gmask);
             const double t_stop = tr[(size_t)(S1 - 1) * kTrajStride];
             const double t_des = t_stop - a.step_back;
             int idx = 0;
@@ -384,7 +428,7 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
             step = idx - 1;
             const double *row = tr + (size_t)step * kTrajStride;
             x = row[0];
-            for (int q = 0; q < 4; ++q) y[q] = row[1 + q];
+            for (int c = 0; c < NC; ++c) y[c] = row[1 + (kDist ? cq : c)];
             pass = 2;
             h = a.fine_step;
             hfix = a.fine_step;
@@ -407,21 +451,40 @@ __global__ void __launch_bounds__(256) k_integrate(IntArgs a)
     }
 }
 
+// One kernel per group size.  Groups of 4+ lanes hold little per-lane state
+// and may use up to 255 registers (one or two warps per SM sub-partition are
+// resident); one- and two-lane groups keep the compiler's default budget so
+// that several warps share each sub-partition.
+template <int G>
+__global__ void __launch_bounds__(256, 1) k_integrate(IntArgs a)
+{
+    integrate_body<G>(a);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_integrate_lane(IntArgs a)
+{
+    integrate_body<G>(a);
+}
+
 template <int G>
 cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
 {
     // no shared memory: give the SM's unified L1/shared storage to L1, where
     // the lanes' coefficient tables and slope arrays live
+    void (*kern)(IntArgs);
+    if constexpr (G >= 4) kern = k_integrate<G>;
+    else kern = k_integrate_lane<G>;
     static bool carveout_set = false;
     if (!carveout_set) {
-        cudaFuncSetAttribute(k_integrate<G>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         carveout_set = true;
     }
     if (grid <= 0) {
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrate<G>, bs, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
         if (per_sm < 1) per_sm = 1;
         // lane groups: at most one warp per SM sub-partition, so that a long
         // binary's group never shares the FP64 pipe; later binaries wait in
@@ -435,7 +498,7 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
         grid = (int)(need < (long long)nsm * per_sm ? need : (long long)nsm * per_sm);
         if (grid < 1) grid = 1;
     }
-    k_integrate<G><<<grid, bs, 0, s>>>(a);
+    kern<<<grid, bs, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -175,7 +175,7 @@ EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, doubl
     FluxShared s;
     s.omega = omega;
     s.v = cbrt(omega);
-    s.lv = log(s.v);
+    s.lv = eob_log(s.v);
     const double vphi_in = 1.0 / (omega_c * omega_c * r * r * r);
     const double vphi = r * cbrt(vphi_in) * omega;
     s.vphi2 = vphi * vphi;
@@ -232,7 +232,7 @@ EOB_HD FluxShared flux_shared_make(const FluxTable &t, double pphi, double omega
     FluxShared s;
     s.omega = omega;
     s.v = v;
-    s.lv = log(v);
+    s.lv = eob_log(v);
     const double vphi = omega / (w * w);
     s.vphi2 = vphi * vphi;
     s.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
@@ -339,7 +339,7 @@ EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, do
 {
     FluxLane f;
     f.v = v;
-    f.lv = log(v);
+    f.lv = eob_log(v);
     const double v2 = v * v, v4 = v2 * v2;
     f.v12 = v4 * v4 * v4;
     const double vphi = omega / (w * w);

@@ -5,10 +5,11 @@
 // (src/EOB.cu:139-222, grad_Ham_align_AD_single) and its second gradient
 // evaluation at p_r = 0 (src/EOB.cu:2611-2616).  Every function of r is
 // carried as a jet (value, d/du) in u = 1/r; the only transcendental calls
-// are one log, two square roots, a reciprocal and the final square roots.
+// are one log (eob_log, fastlog.h), two square roots, a reciprocal and the final square roots.
 // No pow() anywhere: on GB300 one FP64 pow costs about 100 DFMA slots.
 #pragma once
 #include "ham_coeffs.h"
+#include "fastlog.h"
 
 namespace eob {
 
@@ -39,7 +40,7 @@ EOB_HD Jet poly_jet(const double *c, double u)
 EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval *out)
 {
     const double u = 1.0 / r;
-    const double lr = log(r);
+    const double lr = eob_log(r);
     const double su = sqrt(u);
     const double u2 = u * u, u3 = u2 * u, u4 = u3 * u, u5 = u4 * u;
 

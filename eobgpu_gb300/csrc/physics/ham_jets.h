@@ -136,57 +136,103 @@ struct HamPart {
     double H, Hreal, dHdr, dHdpr, dHdL;
 };
 
-EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr, double L)
+// The combination in four pieces, so that two warps carrying one binary can
+// evaluate them side by side (comb_a with comb_b, then comb_even with
+// comb_odd); ham_combine() runs them in sequence.
+
+// A(u) = S Fa As / Dc and the centrifugal coefficient c(u) = u^2 (1 + a^2 Bnpa)
+struct CombA {
+    double idc, Av, Ad, cuv, cud;
+};
+
+EOB_HD CombA comb_a(const HamJets &J, const Jet *jt, double u)
 {
-    const Jet ak0 = jt[J_AK0], aka = jt[J_AKA], fa = jt[J_FA], as = jt[J_AS], dc = jt[J_DC], db = jt[J_DB],
-              g = jt[J_G], bx = jt[J_BX], bnn = jt[J_BNN], q4 = jt[J_Q4], q6 = jt[J_Q6], q8 = jt[J_Q8],
-              n0 = jt[J_N0], n1 = jt[J_N1], n2 = jt[J_N2], n3 = jt[J_N3];
-    const double u2 = u * u, u3 = u2 * u;
-    const double idc = 1.0 / dc.v;
+    const Jet ak0 = jt[J_AK0], aka = jt[J_AKA], fa = jt[J_FA], as = jt[J_AS], dc = jt[J_DC], bnn = jt[J_BNN];
+    const double u2 = u * u;
+    CombA o;
+    o.idc = 1.0 / dc.v;
+    const double idc = o.idc;
     const double Sv = ak0.v + aka.v, Sd = ak0.d + aka.d;
     const double sf = Sv * fa.v;
     const double na = sf * as.v;
     const double dna = fma(Sd * fa.v + Sv * fa.d, as.v, sf * as.d);
-    const double Av = na * idc;
-    const double Ad = fma(-Av, dc.d, dna) * idc;
-
-    const double ad = ak0.v * db.v;
-    const double bnpv = fma(ad, g.v, bx.v);
-    const double bnpd = fma(fma(ak0.d, db.v, ak0.v * db.d), g.v, fma(ad, g.d, bx.d));
+    o.Av = na * idc;
+    o.Ad = fma(-o.Av, dc.d, dna) * idc;
     const double bnpa = bnn.v * idc;
     const double dbnpa = fma(-bnpa, dc.d, bnn.d) * idc;
     const double cf = fma(J.apsq, bnpa, 1.0);
-    const double cuv = u2 * cf;
-    const double cud = fma(2.0 * u, cf, u2 * J.apsq * dbnpa);
+    o.cuv = u2 * cf;
+    o.cud = fma(2.0 * u, cf, u2 * J.apsq * dbnpa);
+    return o;
+}
 
+// B_np(u) and the p_r^4 coefficient q(u, p_r^2)
+struct CombB {
+    double bnpv, bnpd, qa, qad;
+};
+
+EOB_HD CombB comb_b(const Jet *jt, double p2)
+{
+    const Jet ak0 = jt[J_AK0], db = jt[J_DB], g = jt[J_G], bx = jt[J_BX], q4 = jt[J_Q4], q6 = jt[J_Q6],
+              q8 = jt[J_Q8];
+    CombB o;
+    const double ad = ak0.v * db.v;
+    o.bnpv = fma(ad, g.v, bx.v);
+    o.bnpd = fma(fma(ak0.d, db.v, ak0.v * db.d), g.v, fma(ad, g.d, bx.d));
+    o.qa = fma(p2, fma(p2, q8.v, q6.v), q4.v);
+    o.qad = fma(p2, fma(p2, q8.d, q6.d), q4.d);
+    return o;
+}
+
+// a piece of H_eff with its derivatives in u, p_r and L
+struct HeffPart {
+    double v, du, dp, dL;
+};
+
+// even part sqrt(A W) (W = 1 + p_r^2 (1 + B_np) + L^2 c + p_r^4 q)
+EOB_HD HeffPart comb_even(const Jet *jt, const CombA &a, const CombB &b, double pr, double L)
+{
+    const Jet q4 = jt[J_Q4], q6 = jt[J_Q6], q8 = jt[J_Q8];
     const double p2 = pr * pr, L2 = L * L;
-    const double qa = fma(p2, fma(p2, q8.v, q6.v), q4.v);
-    const double qad = fma(p2, fma(p2, q8.d, q6.d), q4.d);
-    const double W = 1.0 + p2 * (1.0 + bnpv) + L2 * cuv + p2 * p2 * qa;
-    const double Wu = p2 * bnpd + L2 * cud + p2 * p2 * qad;
-    const double Wp = 2.0 * pr * ((1.0 + bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
-    const double WL = 2.0 * L * cuv;
-
+    const double W = 1.0 + p2 * (1.0 + b.bnpv) + L2 * a.cuv + p2 * p2 * b.qa;
+    const double Wu = p2 * b.bnpd + L2 * a.cud + p2 * p2 * b.qad;
+    const double Wp = 2.0 * pr * ((1.0 + b.bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
+    const double WL = 2.0 * L * a.cuv;
     // sqrt and the reciprocal from one reciprocal square root
-    const double AW = Av * W;
+    const double AW = a.Av * W;
     const double rAW = eob_rsqrt(AW);
-    const double heven = AW * rAW;
     const double ih2 = 0.5 * rAW;
-    const double hev_u = fma(Ad, W, Av * Wu) * ih2;
-    const double hev_p = Av * Wp * ih2;
-    const double hev_L = Av * WL * ih2;
+    HeffPart o;
+    o.v = AW * rAW;
+    o.du = fma(a.Ad, W, a.Av * Wu) * ih2;
+    o.dp = a.Av * Wp * ih2;
+    o.dL = a.Av * WL * ih2;
+    return o;
+}
 
+// odd part L u^3 N(u, p_r^2) / Dc
+EOB_HD HeffPart comb_odd(const HamJets &J, const Jet *jt, double u, double idc, double pr, double L)
+{
+    const Jet dc = jt[J_DC], n0 = jt[J_N0], n1 = jt[J_N1], n2 = jt[J_N2], n3 = jt[J_N3];
+    const double u2 = u * u, u3 = u2 * u;
+    const double p2 = pr * pr;
     const double n4 = J.n4;
     const double Nv = n0.v + p2 * (n1.v + p2 * (n2.v + p2 * (n3.v + p2 * n4)));
     const double Nu = n0.d + p2 * (n1.d + p2 * (n2.d + p2 * n3.d));
     const double Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * 4.0 * n4));
     const double u3i = u3 * idc;
-    const double hodd = L * u3i * Nv;
-    const double hodd_u = L * idc * (3.0 * u2 * Nv + u3 * Nu - u3 * Nv * idc * dc.d);
-    const double hodd_p = L * u3i * Np * 2.0 * pr;
-    const double hodd_L = u3i * Nv;
+    HeffPart o;
+    o.v = L * u3i * Nv;
+    o.du = L * idc * (3.0 * u2 * Nv + u3 * Nu - u3 * Nv * idc * dc.d);
+    o.dp = L * u3i * Np * 2.0 * pr;
+    o.dL = u3i * Nv;
+    return o;
+}
 
-    const double heff = heven + hodd;
+// H = M sqrt(1 + 2 nu (H_eff - 1)) / nu and its derivatives
+EOB_HD HamPart comb_final(const HamJets &J, double u, const HeffPart &ev, const HeffPart &od)
+{
+    const double heff = ev.v + od.v;
     const double nu = J.nu, M = J.M;
     const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
     const double rs = eob_rsqrt(s2);
@@ -195,16 +241,60 @@ EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr,
     HamPart o;
     o.H = M * s / nu;
     o.Hreal = M * s;
-    o.dHdr = -u2 * f * (hev_u + hodd_u);
-    o.dHdpr = f * (hev_p + hodd_p);
-    o.dHdL = f * (hev_L + hodd_L);
+    o.dHdr = -(u * u) * f * (ev.du + od.du);
+    o.dHdpr = f * (ev.dp + od.dp);
+    o.dHdL = f * (ev.dL + od.dL);
     return o;
+}
+
+EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr, double L)
+{
+    const CombA a = comb_a(J, jt, u);
+    const CombB b = comb_b(jt, pr * pr);
+    const HeffPart ev = comb_even(jt, a, b, pr, L);
+    const HeffPart od = comb_odd(J, jt, u, a.idc, pr, L);
+    return comb_final(J, u, ev, od);
+}
+
+// A jet split in two: the polynomial and sqrt(u) terms, and the log(r) terms
+// (value and d/du each), evaluated by the two warps of a pair; their sum is
+// jet_eval().
+EOB_HD Jet jet_part_cs(const HamJets &J, int j, double u, double r, double su)
+{
+    const double *c = J.c[j], *s = J.s[j];
+    double cv = c[6], cd = 0.0, sv = s[6], sd = 0.0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        cd = fma(cd, u, cv);
+        cv = fma(cv, u, c[k]);
+        sd = fma(sd, u, sv);
+        sv = fma(sv, u, s[k]);
+    }
+    Jet out;
+    out.v = fma(su, sv, cv);
+    out.d = fma(su, fma(0.5 * r, sv, sd), cd);
+    return out;
+}
+
+EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
+{
+    const double *l = J.l[j];
+    double lv = l[6], ld = 0.0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        ld = fma(ld, u, lv);
+        lv = fma(lv, u, l[k]);
+    }
+    Jet out;
+    out.v = lr * lv;
+    out.d = fma(lr, ld, -r * lv);
+    return out;
 }
 
 // Sequential use of the same pieces (host tests, and one-lane callers)
 EOB_HD void ham_eval_jets(const HamJets &J, double r, double pr, double L, HamEval *out)
 {
-    const double u = 1.0 / r, lr = log(r), su = sqrt(u);
+    const double u = 1.0 / r, lr = eob_log(r), su = sqrt(u);
     Jet jt[kNumJets];
     for (int j = 0; j < kNumJets; ++j) jt[j] = jet_eval(J, j, u, r, lr, su);
     const HamPart a = ham_combine(J, jt, u, pr, L);
@@ -226,7 +316,7 @@ __device__ __forceinline__ void ham_eval_group(const HamJets &J, double r, doubl
                                                HamEval *out)
 {
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0, "group size");
-    const double u = 1.0 / r, lr = log(r), su = sqrt(u);
+    const double u = 1.0 / r, lr = eob_log(r), su = sqrt(u);
     constexpr int R = (kNumJets + G - 1) / G;
     double mv[R], md[R];
 #pragma unroll
