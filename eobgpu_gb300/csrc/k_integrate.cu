@@ -26,6 +26,7 @@
 // All loops are bounded: a pass ends after max_tries step attempts, on a
 // non-finite error estimate or step, or at the row capacity.
 #include "eob_device.cuh"
+#include "rhs_pair.cuh"
 
 namespace eob {
 namespace dp {
@@ -134,7 +135,7 @@ __device__ __forceinline__ double pick4(const double v[4], int q)
 }
 
 template <int G>
-__device__ __forceinline__ void integrate_body(const IntArgs &a)
+__device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_all, unsigned long long *bars)
 {
     // G consecutive lanes carry one binary; every lane of the group keeps the
     // same control state, the Hamiltonian jets and flux multipoles are split
@@ -149,14 +150,27 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
     // right-hand side or the stopping rule needs all four; the error norm
     // adds the four components in the reference's order, so every lane
     // reaches the same accept/reject decision with the same bits.
+    //
+    // G = 64: a warp pair per binary (rhs_pair.cuh); each warp runs the
+    // control state of a 32-lane group, role 0 writes the results.
+    constexpr bool kPair = (G == 64);
+    constexpr int GW = kPair ? 32 : G;  // lanes of the group inside one warp
     constexpr bool kDist = (G >= 4);
     constexpr int NC = kDist ? 1 : 4;  // state components held by one lane
     const int lane = threadIdx.x & 31;
-    const int sub = lane & (G - 1);
+    const int sub = lane & (GW - 1);
+    const int role = kPair ? (int)((threadIdx.x >> 5) & 1) : 0;
     const int cq = kDist ? (sub & 3) : 0;  // the component a distributing lane holds
-    const bool leader = (sub == 0);
-    const bool writer = kDist ? (sub < 4) : leader;  // writes trajectory components
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - sub));
+    const bool leader = (sub == 0) && role == 0;
+    const bool writer = kDist ? (sub < 4 && role == 0) : leader;  // writes trajectory components
+    const unsigned gmask = (GW == 32) ? 0xffffffffu : (((1u << GW) - 1u) << (lane - sub));
+    PairXchg *xch = nullptr;
+    PairSync ps{0u, 0u, true};
+    if constexpr (kPair) {
+        const int pair = (int)(threadIdx.x >> 6);
+        xch = &xch_all[pair];
+        ps.bar = (unsigned)__cvta_generic_to_shared(&bars[pair]);
+    }
     // per-lane DOPR853 state (components comp(c) = kDist ? cq : c)
     double k[11][NC];  // slopes k1..k10 (slot 0 unused)
     double y[NC], argl[NC];
@@ -182,7 +196,24 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
         if (phase == kIdle && !queue_empty) {
             unsigned long long slot = 0;
             if (leader) slot = atomicAdd(&a.queue[0], 1ull);
-            if (G > 1) slot = __shfl_sync(gmask, slot, lane - sub);
+            if constexpr (kPair) {
+                if (leader) xch->slot = slot;
+                pair_sync(ps);
+                const unsigned long long got = slot;
+                slot = xch->slot;
+                if (!ps.ok) {
+                    // the partner warp stopped answering: record the binary
+                    // this warp took (if any) and leave
+                    if (leader && got < (unsigned long long)a.B) {
+                        const int bb = a.order ? a.order[got] : (int)got;
+                        a.nsteps[bb] = 1;
+                        a.status[bb] |= EOB_ST_SYNC | EOB_ST_SHORT;
+                    }
+                    break;
+                }
+            } else if (G > 1) {
+                slot = __shfl_sync(gmask, slot, lane - sub);
+            }
             if (slot >= (unsigned long long)a.B) {
                 queue_empty = true;
             } else {
@@ -231,7 +262,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
         double arg[4];
         if constexpr (kDist) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) arg[q] = __shfl_sync(0xffffffffu, argl[0], q, G);
+            for (int q = 0; q < 4; ++q) arg[q] = __shfl_sync(0xffffffffu, argl[0], q, GW);
         } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) arg[q] = argl[q];
@@ -240,7 +271,19 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
         // ------------------------------------------------ the one RHS per loop
         double kk[4];
         if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
+        else if constexpr (kPair) eob_rhs_pair(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
         else eob_rhs_group<G>(rec->jets, rec->flux, arg, kk, sub);
+        if constexpr (kPair) {
+            if (!ps.ok) {
+                // a pair barrier ran out of time: end this binary with what it has
+                if (leader && active) {
+                    a.nsteps[b] = step + 1;
+                    a.status[b] |= st | EOB_ST_SYNC;
+                    a.rhs[b] = n_bin;
+                }
+                break;
+            }
+        }
         if (!active) continue;
         double km[NC];  // this lane's components of the new slope
         if constexpr (kDist) km[0] = pick4(kk, cq);
@@ -291,12 +334,12 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
                 // the four components' terms summed in component order, as
                 // the reference's loop over the equations does
                 const double p1 = e1, p2 = e2;
-                e1 = __shfl_sync(gmask, p1, 0, G);
-                e2 = __shfl_sync(gmask, p2, 0, G);
+                e1 = __shfl_sync(gmask, p1, 0, GW);
+                e2 = __shfl_sync(gmask, p2, 0, GW);
 #pragma unroll
                 for (int q = 1; q < 4; ++q) {
-                    e1 += __shfl_sync(gmask, p1, q, G);
-                    e2 += __shfl_sync(gmask, p2, q, G);
+                    e1 += __shfl_sync(gmask, p1, q, GW);
+                    e2 += __shfl_sync(gmask, p2, q, GW);
                 }
             }
             double denom = e1 + 0.01 * e2;
@@ -458,22 +501,32 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a)
 template <int G>
 __global__ void __launch_bounds__(256, 1) k_integrate(IntArgs a)
 {
-    integrate_body<G>(a);
+    integrate_body<G>(a, nullptr, nullptr);
 }
 
 template <int G>
 __global__ void __launch_bounds__(256) k_integrate_lane(IntArgs a)
 {
-    integrate_body<G>(a);
+    integrate_body<G>(a, nullptr, nullptr);
+}
+
+// warp pairs: blockDim.x a multiple of 64, at most kPairMax pairs
+__global__ void __launch_bounds__(256, 1) k_integrate_pair(IntArgs a)
+{
+    __shared__ PairXchg xch[kPairMax];
+    __shared__ unsigned long long bars[kPairMax];
+    pair_init(bars, (int)(blockDim.x / 64));
+    integrate_body<64>(a, xch, bars);
 }
 
 template <int G>
 cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
 {
-    // no shared memory: give the SM's unified L1/shared storage to L1, where
-    // the lanes' coefficient tables and slope arrays live
+    // little or no shared memory: give the SM's unified L1/shared storage to
+    // L1, where the lanes' coefficient tables and slope arrays live
     void (*kern)(IntArgs);
-    if constexpr (G >= 4) kern = k_integrate<G>;
+    if constexpr (G == 64) kern = k_integrate_pair;
+    else if constexpr (G >= 4) kern = k_integrate<G>;
     else kern = k_integrate_lane<G>;
     static bool carveout_set = false;
     if (!carveout_set) {
@@ -541,7 +594,7 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
     a.max_tries = ra.opt.max_tries > 0 ? ra.opt.max_tries : 2LL * w.L.Lc + 100;
     const int bs = (ra.opt.block > 0 && ra.opt.block <= 256 && ra.opt.block % 32 == 0) ? ra.opt.block : 128;
     int G = ra.opt.lanes_per_binary;
-    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32) G = auto_lanes_per_binary(ra.B);
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32 && G != 64) G = auto_lanes_per_binary(ra.B);
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long) * 8, s);
     if (e != cudaSuccess) return e;
     switch (G) {
@@ -550,7 +603,8 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
         case 4: return launch_g<4>(a, bs, ra.opt.grid, s);
         case 8: return launch_g<8>(a, bs, ra.opt.grid, s);
         case 16: return launch_g<16>(a, bs, ra.opt.grid, s);
-        default: return launch_g<32>(a, bs, ra.opt.grid, s);
+        case 32: return launch_g<32>(a, bs, ra.opt.grid, s);
+        default: return launch_g<64>(a, bs % 64 == 0 ? bs : 128, ra.opt.grid, s);
     }
 }
 

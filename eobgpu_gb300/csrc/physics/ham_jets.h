@@ -256,24 +256,29 @@ EOB_HD HamPart ham_combine(const HamJets &J, const Jet *jt, double u, double pr,
     return comb_final(J, u, ev, od);
 }
 
-// A jet split in two: the polynomial and sqrt(u) terms, and the log(r) terms
-// (value and d/du each), evaluated by the two warps of a pair; their sum is
-// jet_eval().
-EOB_HD Jet jet_part_cs(const HamJets &J, int j, double u, double r, double su)
+// A jet split in pieces that the two warps of a pair evaluate: the
+// polynomial part (P, dP/du) and the sqrt(u) part (su S, su (dS/du + r S / 2))
+// -- jet_half(.., sq = false / true) -- and the log(r) part jet_part_l().
+// poly + sqrt + log, added in that order, is jet_eval().
+EOB_HD Jet jet_half(const HamJets &J, int j, bool sq, double u, double r, double su)
 {
-    const double *c = J.c[j], *s = J.s[j];
-    double cv = c[6], cd = 0.0, sv = s[6], sd = 0.0;
+    const double *c = sq ? J.s[j] : J.c[j];
+    double pv = c[6], pd = 0.0;
 #pragma unroll
     for (int k = 5; k >= 0; --k) {
-        cd = fma(cd, u, cv);
-        cv = fma(cv, u, c[k]);
-        sd = fma(sd, u, sv);
-        sv = fma(sv, u, s[k]);
+        pd = fma(pd, u, pv);
+        pv = fma(pv, u, c[k]);
     }
     Jet out;
-    out.v = fma(su, sv, cv);
-    out.d = fma(su, fma(0.5 * r, sv, sd), cd);
+    out.v = su * pv;
+    out.d = su * (sq ? fma(0.5 * r, pv, pd) : pd);
     return out;
+}
+
+EOB_HD Jet jet_part_cs(const HamJets &J, int j, double u, double r, double su)
+{
+    const Jet a = jet_half(J, j, false, u, r, 1.0), b = jet_half(J, j, true, u, r, su);
+    return {a.v + b.v, a.d + b.d};
 }
 
 EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)

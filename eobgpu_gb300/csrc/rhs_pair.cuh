@@ -1,0 +1,246 @@
+// One binary on two warps (a warp pair): the right-hand side of the EOB
+// equations split into pieces that the two warps evaluate side by side.
+//
+// On GB300 each SM sub-partition issues one FP64 warp-instruction per 64
+// cycles, so a lane group's right-hand side costs as many issue slots as it
+// has FP64 instructions, however many lanes share them.  A binary whose
+// trajectory is the batch's critical path therefore gets shorter only if its
+// instruction stream gets shorter.  The two warps of a pair sit on two
+// sub-partitions of one SM (warps 2p and 2p + 1 of the block), each with its
+// own FP64 pipe, and split every stage whose pieces are independent:
+//
+//   stage        role 0 (warp 2p)                 role 1 (warp 2p + 1)
+//   jets         log r, the log(r) parts          sqrt(u), the polynomial and
+//                                                 sqrt(u) parts (halves of the warp)
+//   combination  A(u), c(u)  -> even part         B_np, q  -> odd part
+//   flux         v = omega^(1/3), log v, v_phi    m factors (m x/(1-e^{-m x}), 4k^2),
+//                powers; multipoles 0..31         y_2/y_3, 1/(8 pi nu); multipoles 32..34
+//
+// Values cross between the warps through shared memory at five pair
+// barriers per right-hand side (an mbarrier of 64 arrivals, waited on with a
+// time limit: if the partner does not arrive within kPairTimeoutNs the pair
+// reports failure and the integrator ends that binary with EOB_ST_SYNC).
+// Every value both warps go on to use is read by both from shared memory
+// (never one warp's register copy, which the compiler could fuse into a later
+// fma differently), so their results -- and every later control decision of
+// the integrator, which both warps run redundantly -- are bitwise identical.
+#pragma once
+#include "physics/flux_eval.h"
+
+namespace eob {
+
+constexpr int kPairMax = 4;                                  // pairs per block (256 threads)
+constexpr unsigned long long kPairTimeoutNs = 2000000000ull;  // 2 s per barrier wait
+constexpr int kPairMaxPolls = 1 << 28;                        // and at most this many polls
+
+// shared-memory exchange of one pair
+struct PairXchg {
+    double jet[2][2][32];  // [part: 0 log, 1 poly+sqrt][v, d][lane]
+    double b[4][32];       // role 1 -> 0: bnpv, bnpd, qa, qad
+    double ev[4][32];      // role 0 -> both: even part of H_eff and its derivatives
+    double od[4][32];      // role 1 -> both: odd part
+    double T[8], k4[8];    // role 1 -> 0: m factors, m = 1..8
+    double fl[13];         // role 0 -> 1: v, log v, v^12, S_even, S_odd, v_phi^(2e) e = 2..9
+    double part[2];        // flux partial sums of the two warps
+    double aux[2];         // role 1 -> both: y_2 / y_3, 1 / (8 pi nu)
+    unsigned long long slot;
+};
+
+struct PairSync {
+    unsigned bar;     // shared-memory address of the pair's mbarrier
+    unsigned parity;  // parity of the phase this warp waits for next
+    bool ok;          // false once a wait ran out of time
+};
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Both warps of the pair arrive (all 64 lanes: each lane's shared and global
+// writes before the barrier are released to the other warp) and wait, with a
+// time limit, for the phase to complete.
+__device__ __forceinline__ void pair_sync(PairSync &ps)
+{
+    if (!ps.ok) return;
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(ps.bar) : "memory");
+    unsigned done = 0;
+    unsigned long long t0 = 0;
+    for (int i = 0;; ++i) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(ps.bar), "r"(ps.parity)
+            : "memory");
+        if (done) break;
+        if (i == 0) t0 = global_ns();
+        else if (global_ns() - t0 > kPairTimeoutNs || i >= kPairMaxPolls) break;
+    }
+    ps.parity ^= 1u;
+    if (!__all_sync(0xffffffffu, done)) ps.ok = false;
+}
+
+// Set-up by the block's first thread, before any pair barrier is used.
+__device__ __forceinline__ void pair_init(unsigned long long *bars, int npairs)
+{
+    if (threadIdx.x == 0) {
+        for (int p = 0; p < npairs; ++p) {
+            const unsigned a = (unsigned)__cvta_generic_to_shared(&bars[p]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(64) : "memory");
+        }
+    }
+    __syncthreads();
+}
+
+// multipoles at sorted positions [FIRST, FIRST + 32) of one warp, m factors
+// from shared memory
+template <int FIRST>
+__device__ __forceinline__ double flux_warp_modes(const FluxTable &t, const FluxLane &f, const PairXchg &x, int lane)
+{
+    constexpr int KM = kFluxDegSorted[FIRST];
+    const int pos = FIRST + lane;
+    const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
+    const int m = lm_packed(i) & 15;
+    const double here = flux_mode_lane<KM>(t, i, f, x.T[m - 1], x.k4[m - 1]);
+    return (pos < kNumLM) ? here : 0.0;
+}
+
+// k = f(y) for the binary of this pair; both warps call it with the same y
+// and return the same k.  role: 0 or 1; lane: 0..31.
+__device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &t, const double y[4], double k[4],
+                                             int lane, int role, PairXchg &x, PairSync &ps)
+{
+    const double r = y[0], L = y[3];
+    const int j = lane & 15;
+    const double u = 1.0 / r;
+
+    // ---- jets: role 0 the log(r) parts; role 1 the polynomial parts on
+    // lanes 0..15 and the sqrt(u) parts on lanes 16..31
+    if (role == 0) {
+        const double lr = eob_log(r);
+        const Jet p = jet_part_l(J, j, u, r, lr);
+        x.jet[0][0][lane] = p.v;
+        x.jet[0][1][lane] = p.d;
+    } else {
+        const bool sq = lane >= 16;
+        const Jet hj = jet_half(J, j, sq, u, r, sq ? sqrt(u) : 1.0);
+        const double ov = __shfl_xor_sync(0xffffffffu, hj.v, 16);
+        const double od = __shfl_xor_sync(0xffffffffu, hj.d, 16);
+        // lanes j and j + 16 hold the two halves; add them in one order
+        x.jet[1][0][lane] = sq ? ov + hj.v : hj.v + ov;
+        x.jet[1][1][lane] = sq ? od + hj.d : hj.d + od;
+    }
+    pair_sync(ps);  // 1: jets
+    const double jv = x.jet[1][0][lane] + x.jet[0][0][lane];
+    const double jd = x.jet[1][1][lane] + x.jet[0][1][lane];
+    Jet jt[kNumJets];
+#pragma unroll
+    for (int q = 0; q < kNumJets; ++q) {
+        jt[q].v = __shfl_sync(0xffffffffu, jv, q);
+        jt[q].d = __shfl_sync(0xffffffffu, jd, q);
+    }
+
+    // ---- combination (odd lanes at p_r = 0: the circular frequency)
+    const double pr = (lane & 1) ? 0.0 : y[2];
+    if (role == 0) {
+        const CombA a = comb_a(J, jt, u);
+        pair_sync(ps);  // 2: B_np, q
+        CombB b;
+        b.bnpv = x.b[0][lane];
+        b.bnpd = x.b[1][lane];
+        b.qa = x.b[2][lane];
+        b.qad = x.b[3][lane];
+        const HeffPart e = comb_even(jt, a, b, pr, L);
+        x.ev[0][lane] = e.v;
+        x.ev[1][lane] = e.du;
+        x.ev[2][lane] = e.dp;
+        x.ev[3][lane] = e.dL;
+        pair_sync(ps);  // 3: even and odd parts
+    } else {
+        const CombB b = comb_b(jt, pr * pr);
+        x.b[0][lane] = b.bnpv;
+        x.b[1][lane] = b.bnpd;
+        x.b[2][lane] = b.qa;
+        x.b[3][lane] = b.qad;
+        if (lane == 0) {
+            x.aux[0] = y[2] / y[3];
+            x.aux[1] = 1.0 / (8.0 * kPi * J.nu);
+        }
+        pair_sync(ps);  // 2
+        const HeffPart o = comb_odd(J, jt, u, 1.0 / jt[J_DC].v, pr, L);
+        x.od[0][lane] = o.v;
+        x.od[1][lane] = o.du;
+        x.od[2][lane] = o.dp;
+        x.od[3][lane] = o.dL;
+        pair_sync(ps);  // 3
+    }
+    HeffPart ev, od;
+    ev.v = x.ev[0][lane];
+    ev.du = x.ev[1][lane];
+    ev.dp = x.ev[2][lane];
+    ev.dL = x.ev[3][lane];
+    od.v = x.od[0][lane];
+    od.du = x.od[1][lane];
+    od.dp = x.od[2][lane];
+    od.dL = x.od[3][lane];
+    const HamPart hp = comb_final(J, u, ev, od);
+    const double Hreal = __shfl_sync(0xffffffffu, hp.Hreal, 0);
+    const double dHdr = __shfl_sync(0xffffffffu, hp.dHdr, 0);
+    const double dHdpr = __shfl_sync(0xffffffffu, hp.dHdpr, 0);
+    const double omega = __shfl_sync(0xffffffffu, hp.dHdL, 0);
+    const double omega_c = __shfl_sync(0xffffffffu, hp.dHdL, 1);
+
+    // ---- flux
+    double part;
+    if (role == 0) {
+        // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction stream
+        const double cr = cbrt((lane & 1) ? omega_c : omega);
+        const double v = __shfl_sync(0xffffffffu, cr, 0), w = __shfl_sync(0xffffffffu, cr, 1);
+        const FluxLane f = flux_lane_make(t, L, omega, Hreal, v, w);
+        if (lane == 0) {
+            x.fl[0] = f.v;
+            x.fl[1] = f.lv;
+            x.fl[2] = f.v12;
+            x.fl[3] = f.Se;
+            x.fl[4] = f.Sodd;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) x.fl[5 + q] = f.vp[q];
+        }
+        pair_sync(ps);  // 4: FluxLane and m factors
+        part = flux_warp_modes<0>(t, f, x, lane);
+    } else {
+        double Tm, k4m;
+        flux_m_factors((lane & 7) + 1, 4.0 * kPi * Hreal * omega, Hreal * omega, &Tm, &k4m);
+        if (lane < 8) {
+            x.T[lane] = Tm;
+            x.k4[lane] = k4m;
+        }
+        pair_sync(ps);  // 4
+        FluxLane f;
+        f.v = x.fl[0];
+        f.lv = x.fl[1];
+        f.v12 = x.fl[2];
+        f.Se = x.fl[3];
+        f.Sodd = x.fl[4];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) f.vp[q] = x.fl[5 + q];
+        part = flux_warp_modes<32>(t, f, x, lane);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if (lane == 0) x.part[role] = part;
+    pair_sync(ps);  // 5: flux partial sums
+    const double total = x.part[0] + x.part[1];
+    // F / omega with F = total omega^2 / (8 pi) / nu
+    const double fo = total * omega * x.aux[1];
+    k[0] = dHdpr;
+    k[1] = omega;
+    k[2] = -dHdr - x.aux[0] * fo;
+    k[3] = -fo;
+}
+
+}  // namespace eob

@@ -39,6 +39,88 @@ void phys_ham_jets(const double *st, const double *add, int n, double *out)
     }
 }
 
+// the same through the pieces two warps of a pair evaluate side by side
+// (jet halves + log part, comb_a/comb_b, comb_even/comb_odd, comb_final)
+void phys_ham_pair(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, add[i], add[n + i], add[2 * n + i], add[3 * n + i], add[5 * n + i], add[6 * n + i],
+                              add[7 * n + i], add[8 * n + i]);
+        eob::HamJets J;
+        eob::ham_jets_build(h, &J);
+        const double r = st[i], L = st[3 * n + i];
+        const double u = 1.0 / r, lr = eob::eob_log(r), su = sqrt(u);
+        eob::Jet jt[eob::kNumJets];
+        for (int j = 0; j < eob::kNumJets; ++j) {
+            const eob::Jet a = eob::jet_half(J, j, false, u, r, 1.0), b = eob::jet_half(J, j, true, u, r, su);
+            const eob::Jet l = eob::jet_part_l(J, j, u, r, lr);
+            jt[j].v = (a.v + b.v) + l.v;
+            jt[j].d = (a.d + b.d) + l.d;
+        }
+        double res[2][5];
+        for (int z = 0; z < 2; ++z) {
+            const double pr = z ? 0.0 : st[2 * n + i];
+            const eob::CombA ca = eob::comb_a(J, jt, u);
+            const eob::CombB cb = eob::comb_b(jt, pr * pr);
+            const eob::HeffPart ev = eob::comb_even(jt, ca, cb, pr, L);
+            const eob::HeffPart od = eob::comb_odd(J, jt, u, 1.0 / jt[eob::J_DC].v, pr, L);
+            const eob::HamPart hp = eob::comb_final(J, u, ev, od);
+            res[z][0] = hp.H; res[z][1] = hp.dHdr; res[z][2] = hp.dHdpr; res[z][3] = hp.dHdL; res[z][4] = hp.Hreal;
+        }
+        out[5 * i + 0] = res[0][0]; out[5 * i + 1] = res[0][1]; out[5 * i + 2] = res[0][2];
+        out[5 * i + 3] = res[0][3]; out[5 * i + 4] = res[1][3];
+    }
+}
+
+// flux as a warp pair sums it: multipoles at sorted positions 0..31 (one
+// warp) and 32..34 (the other), m factors per m, shared pieces from the two
+// cube roots
+static double flux_pair_host(const eob::FluxTable &t, double pphi, double omega, double Hreal, double omega_c)
+{
+    const eob::FluxLane f = eob::flux_lane_make(t, pphi, omega, Hreal, cbrt(omega), cbrt(omega_c));
+    double T[8], k4[8];
+    for (int m = 1; m <= 8; ++m)
+        eob::flux_m_factors(m, 4.0 * eob::kPi * Hreal * omega, Hreal * omega, &T[m - 1], &k4[m - 1]);
+    static const signed char order[35] = {0, 1, 4, 3, 2, 8, 7, 6, 5, 13, 11, 9, 12, 10, 19, 17, 15, 18,
+                                          16, 14, 26, 24, 22, 20, 25, 23, 21, 34, 33, 32, 31, 30, 29, 28, 27};
+    double part[2] = {0.0, 0.0};
+    for (int pos = 0; pos < 35; ++pos) {
+        const int idx = order[pos];
+        const int m = eob::lm_packed(idx) & 15;
+        part[pos >= 32] += eob::flux_mode_lane<10>(t, idx, f, T[m - 1], k4[m - 1]);
+    }
+    return (part[0] + part[1]) * omega * omega / (8.0 * eob::kPi);
+}
+
+void phys_flux_pair(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        const double m1 = add[i], m2 = add[n + i], c1 = add[2 * n + i], c2 = add[3 * n + i];
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, m1, m2, c1, c2, 0, 0, 0, 0);
+        const double eta = m1 * m2 / ((m1 + m2) * (m1 + m2));
+        const double chiS = 0.5 * (c1 + c2), chiA = 0.5 * (c1 - c2);
+        const double tpl = (1.0 - 2.0 * eta) * chiS + (m1 - m2) / (m1 + m2) * chiA;
+        static eob::FacCoeffs fc;
+        eob::fac_coeffs_build(&fc, 1, m1, m2, eta, tpl, chiS, chiA);
+        double pre_re[35], pre_im[35];
+        for (int j = 0; j < 35; ++j) { pre_re[j] = add[(10 + 2 * j) * n + i]; pre_im[j] = add[(11 + 2 * j) * n + i]; }
+        static eob::FluxTable t;
+        eob::flux_table_build(&t, fc, pre_re, pre_im, 0.0, h.nu);
+        eob::HamEval e;
+        eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
+        out[2 * i] = eob::flux_eval_lanes(t, st[3 * n + i], e.dHdL, e.Hreal, e.omega_c);
+        out[2 * i + 1] = flux_pair_host(t, st[3 * n + i], e.dHdL, e.Hreal, e.omega_c);
+    }
+}
+
+// the hot path's logarithm
+void phys_log(const double *x, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) out[i] = eob::eob_log(x[i]);
+}
+
 // ODE right-hand side with coefficient tables built for each point's binary
 void phys_rhs(const double *st, const double *add, int n, double *k)
 {
