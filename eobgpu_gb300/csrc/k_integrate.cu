@@ -555,9 +555,10 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// Lanes per binary: a power of two in [1, 32].  One lane per binary is the
-// most efficient use of the FP64 pipe; more lanes per binary shorten each
-// binary's critical path when the batch cannot fill the device.
+// Lanes per binary: a power of two in [1, 64] (64: a warp pair).  One lane
+// per binary is the most efficient use of the FP64 pipe; more lanes per
+// binary shorten each binary's critical path when the batch cannot fill the
+// device.
 int auto_lanes_per_binary(int B)
 {
     int dev = 0, nsm = 0;
@@ -566,10 +567,15 @@ int auto_lanes_per_binary(int B)
     // up to two warps' worth of lanes per SM sub-partition: the grid keeps one
     // warp per sub-partition resident and the work queue feeds it the rest,
     // longest binaries first, so a batch bound by its longest binary gets the
-    // shortest chain (e.g. B = 1024 -> 32 lanes, B = 4096 -> 8 lanes)
+    // shortest chain (e.g. B = 4096 -> 8 lanes)
     const long long target = (long long)nsm * 4 * 32 * 2;
     int G = 1;
     while (G < 32 && (long long)B * (G * 2) <= target) G *= 2;
+    // warp pairs cost about 1.3x the issue slots of a 32-lane group per
+    // right-hand side but shorten the chain 1.5x: worth it while the batch's
+    // total work stays below its longest binary's chain (up to four warps'
+    // worth of lanes per sub-partition, e.g. B = 1024 -> 64)
+    if (G == 32 && (long long)B * 64 <= 2 * target) G = 64;
     return G;
 }
 
