@@ -52,6 +52,21 @@ def _census_flops():
 
 F_RHS = _census_flops()
 
+TRAFFIC = os.path.join(ROOT, "profiles", "k_integrate_pair_traffic_config2.md")
+
+
+def _traffic_bytes():
+    """DRAM bytes (read + write) of one integrator launch on the default
+    workload, from the committed ncu capture (profiles/)."""
+    try:
+        with open(TRAFFIC) as f:
+            for line in f:
+                if line.startswith("TRAFFIC_BYTES_PER_LAUNCH"):
+                    return int(line.split("=")[1].strip())
+    except OSError:
+        pass
+    return None
+
 
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -478,6 +493,7 @@ def main():
         torch.cuda.synchronize()
         e2e_ms = [a.elapsed_time(b) for a, b in ev2]
     clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
     t_dev = max_over_ranks(float(np.sum(step_ms)), ws, device)
     t_e2e = max_over_ranks(float(np.sum(e2e_ms)), ws, device)
     value = B * ws * args.steps / (t_dev / 1e3)
@@ -510,9 +526,13 @@ def main():
     # the integrator's critical path: the binary with the most right-hand sides
     rhs_b = wl.rhs_counts()
     crit = int(rhs_b.max()) if len(rhs_b) else 0
+    us_rhs = 1e3 * stage_ms["integrate"] / max(1, crit)
     critical = {"binary_rhs_max": crit, "binary_rhs_median": float(np.median(rhs_b)) if len(rhs_b) else 0.0,
                 "rhs_total": int(rhs_b.sum()),
-                "integrate_us_per_rhs_on_path": 1e3 * stage_ms["integrate"] / max(1, crit)}
+                "integrate_us_per_rhs_on_path": us_rhs,
+                # the chain's length in FP64 issue slots of one SM sub-partition
+                # (one FP64 warp instruction per 64 cycles at the sampled clock)
+                "fp64_slots_per_rhs_on_path": us_rhs * sm_mhz / 64.0}
     # FP64 peak of this device, measured
     nsm = torch.cuda.get_device_properties(device).multi_processor_count
     pk_out = torch.empty(nsm * 8 * 256, dtype=torch.float64, device=device)
@@ -529,8 +549,12 @@ def main():
     roof = None
     if F_RHS:
         achieved = F_RHS * cnt["rhs_binaries"] / (stage_ms["integrate"] / 1e3) / 1e12
+        default_workload = args.config == 2 and not args.batch and not args.lanes
         roof = {"kernel": "k_integrate", "bound": "fp64", "achieved": achieved, "peak": fp64_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                "traffic": _traffic_bytes() if default_workload else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                  "profiles/k_integrate_pair_traffic_config2.md" if default_workload else None,
                 "peak_source": "measured live: FP64 DFMA probe (eob_fp64_probe), burst",
                 "work": f"{F_RHS:.0f} FP64 FLOP per RHS x {cnt['rhs_binaries']} RHS evaluations",
                 "lane_occupancy": cnt["rhs_binaries"] / max(1, cnt["rhs_all_lanes"])}
