@@ -300,6 +300,86 @@ def run_plain(args, cfg, local):
                                                                "rows_max": int(ns.max().item())})}))
 
 
+def run_op(args, local):
+    """Reference-shaped kernels outside the fused path, timed alone on
+    synthetic inputs of the benchmark's shapes (B = 1024 binaries, N = 2^17
+    samples or 2^16 + 1 frequency bins): --op tdinterp2 (mode synthesis on the
+    uniform grid, TD2) or --op fd_lnl (frequency-domain likelihood partials,
+    three detectors).  Reports the kernel time, algorithmic bytes and the
+    fraction of the measured HBM bandwidth; both kernels evaluate one FP64
+    sincos per output (per mode for TD2), so they are FP64-issue bound."""
+    import torch
+    from eobgpu_gb300.eob import pytdinterp
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    g = torch.Generator(device="cpu").manual_seed(7)
+    B = args.batch or 1024
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    if args.op == "tdinterp2":
+        K = len(workload.CONFIGS[3].modes) if args.config == 3 else 1
+        N, L = 131072, 4096
+        dt = 1.0 / 2048
+        ts = (torch.arange(L, dtype=torch.float64) * (N * dt / (L - 1))).repeat(B).to(device)
+        nsubs = 2 * K + 1
+        arrs = [torch.randn(B * nsubs * L, generator=g, dtype=torch.float64).to(device) for _ in range(4)]
+        tgrid = torch.arange(N, dtype=torch.float64, device=device) * dt
+        lengths = torch.full((B,), N, dtype=torch.int32, device=device)
+        inds = torch.clamp(torch.searchsorted(ts[:L].contiguous(), tgrid, right=True) - 1, 0, L - 1).to(torch.int32)
+        inds = inds.repeat(B)
+        old = torch.full((B,), L, dtype=torch.int32, device=device)
+        ms = torch.tensor([2, 1, 3, 4, 5][:K], dtype=torch.int32, device=device)
+        out = torch.empty(B * N, dtype=torch.complex128, device=device)
+
+        def once():
+            pytdinterp.TDInterp_wrap2(out, tgrid, ts, *arrs, L, old, N, B, K, ms, ms, inds, lengths, N)
+        units = B * N
+        byts = units * (16 + 4 + 8) + B * nsubs * L * 32 + B * L * 8
+        work = f"{B} binaries x {N} samples, {K} mode(s): write 16 B, read index 4 B and time 8 B per sample, " \
+               f"spline tables once"
+    else:
+        nch, N = 3, 65537
+        hp = torch.randn(B * N, dtype=torch.complex128, generator=g).to(device)
+        hc = torch.randn(B * N, dtype=torch.complex128, generator=g).to(device)
+        data = torch.randn(nch * N, dtype=torch.complex128, generator=g).to(device)
+        psd = (torch.rand(nch * N, dtype=torch.float64, generator=g) + 0.5).to(device)
+        F = [torch.rand(nch * B, dtype=torch.float64, generator=g).to(device) for _ in range(3)]
+        temp = torch.empty(((N + 1023) // 1024) * B * nch, dtype=torch.complex128, device=device)
+
+        def once():
+            pytdinterp.all_in_one_likelihood(temp, hp, hc, data, psd, F[0], F[1], F[2] * 0.01, 0.125, B, nch, N)
+        units = B * N
+        byts = units * 32 + nch * N * 24 + temp.numel() * 16
+        work = f"{B} binaries x {N} bins x {nch} detectors: templates 32 B per (binary, bin) read once, " \
+               f"data and PSD per detector"
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        once()
+    torch.cuda.synchronize()
+    ms_l = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        once()
+        e1.record()
+        torch.cuda.synchronize()
+        ms_l.append(e0.elapsed_time(e1))
+    t = float(np.median(ms_l))
+    achieved = byts / (t / 1e3) / 1e9
+    print(json.dumps({"op": args.op, "metric": "outputs/s", "value": units / (t / 1e3), "unit": "outputs/s",
+                      "ms": t, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                   "frac": achieved / hbm, "traffic": None, "work": work,
+                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+                      "l2": "flushed between timed launches (256 MiB write)"}))
+
+
 def run_serving(args, ws, rank, local):
     """Configuration 4: a seeded Poisson trace of walker requests (1..512
     binaries each, 80 % from a ball around the injection, 20 % from the
@@ -376,6 +456,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="integrator lanes per binary (0: chosen from the batch size)")
+    ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl"],
+                    help="time one reference-shaped kernel alone (mode synthesis TD2, or FD likelihood partials)")
     ap.add_argument("--census", action="store_true",
                     help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
     args = ap.parse_args()
@@ -397,6 +479,9 @@ def main():
     ws, rank, local = dist_init()
     if args.impl == "plain":
         run_plain(args, cfg, local)
+        return
+    if args.op:
+        run_op(args, local)
         return
     if args.config == 4:
         run_serving(args, ws, rank, local)

@@ -51,6 +51,7 @@ _SIGS = {
     "eob_workspace_counters": (c_int, [_P, c_int, c_int, c_int, c_int, _P, _P]),
     "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
     "eob_component_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
+    "eob_pair_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
     "eob_noalloc_scratch_bytes": (c_size_t, []),
     "eob_waveform_lnl_noalloc": (c_int, [_P, c_int, _P, _P, c_int, c_double, _P, c_int, c_double,
                                          ctypes.POINTER(EobOptions), _P, _P, _P]),
@@ -72,6 +73,9 @@ _SIGS = {
     "eob_dopr853_error": (c_int, [_P] * 12 + [c_int, c_int, _P]),
     "eob_dopr853_controller": (c_int, [_P] * 6 + [c_int, c_int, _P]),
     "eob_interpolate_td": (c_int, [_P] * 7 + [c_int, c_int, _P]),
+    "eob_tdinterp2": (c_int, [_P] * 7 + [c_int, _P, c_int, c_int, c_int, _P, _P, _P, _P, c_int, _P]),
+    "eob_tdinterp": (c_int, [_P] * 8 + [c_int, c_int, c_int, _P, _P, _P, _P, _P, _P]),
+    "eob_all_in_one_likelihood": (c_int, [_P] * 8 + [c_double, c_int, c_int, c_int, _P]),
 }
 
 _lib = None

@@ -1,6 +1,7 @@
 // FP64 issue-rate probe used by the benchmark to measure the denominator of
 // the integrator's roofline on the device it runs on.
 #include "eob_device.cuh"
+#include "rhs_pair.cuh"
 
 namespace {
 __global__ void k_fp64_probe(double *out, int iters)
@@ -60,6 +61,54 @@ __global__ void k_component(const eob::BinaryRec *bins, int iters, double *out)
         }
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+// Round trip of the warp-pair barrier: every pair of the block passes `iters`
+// barriers back to back (mode 0: suspending try_wait, as the integrator; mode
+// 1: spinning test_wait); out[pair] = 1 if every wait completed in time.
+__global__ void k_pair_sync_probe(int iters, int mode, int *out)
+{
+    __shared__ unsigned long long bars[eob::kPairMax];
+    eob::pair_init(bars, (int)(blockDim.x / 64));
+    const int pair = (int)(threadIdx.x >> 6);
+    eob::PairSync ps{(unsigned)__cvta_generic_to_shared(&bars[pair]), 0u, true};
+    for (int i = 0; i < iters; ++i) {
+        if (mode == 0) eob::pair_sync(ps);
+        else eob::pair_sync_spin(ps);
+    }
+    if ((threadIdx.x & 63) == 0) out[blockIdx.x * eob::kPairMax + pair] = ps.ok ? 1 : 0;
+}
+
+// Warp-pair right-hand side alone: each pair evaluates it `iters` times on
+// binary 0 of a prepared workspace (state varied slightly), out[pair] = sum.
+__global__ void k_pair_rhs_probe(const eob::BinaryRec *bins, int iters, double *out)
+{
+    __shared__ eob::PairXchg xch[eob::kPairMax];
+    __shared__ unsigned long long bars[eob::kPairMax];
+    eob::pair_init(bars, (int)(blockDim.x / 64));
+    const int pair = (int)(threadIdx.x >> 6), role = (int)((threadIdx.x >> 5) & 1), lane = threadIdx.x & 31;
+    eob::PairSync ps{(unsigned)__cvta_generic_to_shared(&bars[pair]), 0u, true};
+    const eob::BinaryRec &b = bins[0];
+    double r = 12.0 + 1e-3 * pair, acc = 0.0;
+    for (int i = 0; i < iters; ++i) {
+        r += 1e-9;
+        const double y[4] = {r, 0.0, -1e-3, 3.9};
+        double k[4];
+        eob::eob_rhs_pair(b.jets, b.flux, y, k, lane, role, xch[pair], ps);
+        acc += k[0] + k[1] + k[2] + k[3];
+    }
+    if ((threadIdx.x & 63) == 0) out[blockIdx.x * eob::kPairMax + pair] = ps.ok ? acc : 0.0;
+}
+
+extern "C" int eob_pair_probe(const void *bins, int which, int iters, void *out, int blocks, int threads,
+                              cudaStream_t stream)
+{
+    if (!out || blocks < 1 || threads < 64 || threads > 64 * eob::kPairMax || threads % 64 || iters < 1)
+        return EOB_E_ARG;
+    if (which == 0 || which == 1) k_pair_sync_probe<<<blocks, threads, 0, stream>>>(iters, which, (int *)out);
+    else if (which == 2 && bins) k_pair_rhs_probe<<<blocks, threads, 0, stream>>>((const eob::BinaryRec *)bins, iters, (double *)out);
+    else return EOB_E_ARG;
+    return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 
 extern "C" int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,

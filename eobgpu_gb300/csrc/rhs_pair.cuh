@@ -84,6 +84,33 @@ __device__ __forceinline__ void pair_sync(PairSync &ps)
     if (!__all_sync(0xffffffffu, done)) ps.ok = false;
 }
 
+// The same barrier polled with the non-suspending test (a warp that waits
+// spins on its own sub-partition, where it is the only warp).
+__device__ __forceinline__ void pair_sync_spin(PairSync &ps)
+{
+    if (!ps.ok) return;
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(ps.bar) : "memory");
+    unsigned done = 0;
+    unsigned long long t0 = 0;
+    for (int i = 0;; ++i) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(ps.bar), "r"(ps.parity)
+            : "memory");
+        if (done) break;
+        if ((i & 255) == 0) {
+            if (i == 0) t0 = global_ns();
+            else if (global_ns() - t0 > kPairTimeoutNs) break;
+        }
+        if (i >= kPairMaxPolls) break;
+    }
+    ps.parity ^= 1u;
+    if (!__all_sync(0xffffffffu, done)) ps.ok = false;
+}
+
 // Set-up by the block's first thread, before any pair barrier is used.
 __device__ __forceinline__ void pair_init(unsigned long long *bars, int npairs)
 {

@@ -155,6 +155,27 @@ class CubicSplineInterpolantTD:
     def _shaped(self, a):
         return a.view(self.max_length, self.nsubs, self.num_bin_all).permute(2, 1, 0)
 
+    # [B][nsubs][L] views, as the reference's properties (eob/seobnrv4phm.py:221-239)
+    @property
+    def y_shaped(self):
+        return self._shaped(self.y)
+
+    @property
+    def c1_shaped(self):
+        return self._shaped(self.c1)
+
+    @property
+    def c2_shaped(self):
+        return self._shaped(self.c2)
+
+    @property
+    def c3_shaped(self):
+        return self._shaped(self.c3)
+
+    @property
+    def container(self):
+        return [self.x, self.y, self.c1, self.c2, self.c3]
+
     def __call__(self, tnew, deriv_order=0):
         tnew = _cuda(tnew)
         if tnew.ndim != 2 or tnew.shape[0] != self.num_bin_all:
@@ -179,6 +200,72 @@ class CubicSplineInterpolantTD:
         else:
             raise ValueError("deriv_order must be within 0 <= deriv_order <= 3.")
         return out.squeeze()
+
+
+class TDInterp:
+    """Mode synthesis from spline containers on a uniform time grid
+    (eob/seobnrv4phm.py:389-500) through TDInterp_wrap2: per binary the
+    samples before its last knot, each mode spline rotated by e^{-i m phi} and
+    summed.  Returns the flat complex template carrier [numBinAll * data_length]."""
+
+    def __init__(self, max_init_len=-1, use_gpu=True):
+        if not use_gpu:
+            raise ValueError("this implementation runs on the GPU only (no CPU fallback)")
+        if max_init_len > 0:
+            # as the reference: buffers are not implemented
+            raise NotImplementedError
+        self.use_buffers = False
+        self.template_gen = pytdinterp.TDInterp_wrap2
+
+    @property
+    def template_channels(self):
+        return [self.template_carrier[i].reshape(self.data_length) for i in range(self.num_bin_all)]
+
+    def __call__(self, dataTime, interp_container, length, data_length, num_modes, ls, ms, numBinAll, dt=1 / 1024):
+        self.length, self.num_modes, self.num_bin_all, self.data_length = length, num_modes, numBinAll, data_length
+        dataTime = _cuda(dataTime)
+        ts = interp_container.t_shaped
+        ends = ts.max(dim=1).values
+        st = torch.searchsorted(dataTime, torch.zeros_like(ends), right=False)
+        et = torch.searchsorted(dataTime, ends.contiguous(), right=False)
+        self.lengths = et.to(torch.int32)
+        max_length = int(self.lengths.max().item())
+        inds = torch.zeros(self.num_bin_all * max_length, dtype=torch.int32, device="cuda")
+        old_lengths = interp_container.lengths
+        old_length = int(old_lengths.max().item())
+        for i in range(self.num_bin_all):
+            a, e = int(st[i]), int(et[i])
+            inds[i * max_length + a: i * max_length + e] = (
+                torch.searchsorted(ts[i].contiguous(), dataTime[a:e].contiguous(), right=True).to(torch.int32) - 1)
+        self.template_carrier = torch.zeros(int(data_length * self.num_bin_all), dtype=torch.complex128, device="cuda")
+        ls = _cuda(ls, torch.int32)
+        ms = _cuda(ms, torch.int32)
+        self.template_gen(self.template_carrier, dataTime, ts.contiguous().flatten(),
+                          interp_container.y_shaped.contiguous().flatten(),
+                          interp_container.c1_shaped.contiguous().flatten(),
+                          interp_container.c2_shaped.contiguous().flatten(),
+                          interp_container.c3_shaped.contiguous().flatten(), old_length, old_lengths, self.data_length,
+                          self.num_bin_all, self.num_modes, ls, ms, inds, self.lengths, max_length)
+        return self.template_carrier
+
+
+def fd_likelihood(hp_fd, hc_fd, data, psd, Fplus, Fcross, time_shift, df, num_bin_all, nchannels, return_complex=False):
+    """The likelihood step of BBHWaveformFD.get_ll (eob/seobnrv4phm.py:778-817):
+    per-1024-bin partials from all_in_one_likelihood, then
+    lnL = -1/2 df 4 sum over blocks and channels.  hp_fd, hc_fd: complex
+    [num_bin_all, N]; data, psd: [nchannels, N]; Fplus, Fcross, time_shift:
+    [nchannels, num_bin_all] (flattened as the reference does)."""
+    hp = _cuda(hp_fd, torch.complex128).reshape(-1)
+    hc = _cuda(hc_fd, torch.complex128).reshape(-1)
+    d = _cuda(data, torch.complex128).reshape(-1)
+    S = _cuda(psd).reshape(-1)
+    N = hp.numel() // num_bin_all
+    nblk = -(-N // 1024)
+    temp = torch.zeros(nblk * num_bin_all * nchannels, dtype=torch.complex128, device="cuda")
+    pytdinterp.all_in_one_likelihood(temp, hp, hc, d, S, _cuda(Fplus).reshape(-1), _cuda(Fcross).reshape(-1),
+                                     _cuda(time_shift).reshape(-1), df, num_bin_all, nchannels, N)
+    like = -1.0 / 2.0 * df * 4.0 * temp.reshape(-1, num_bin_all, nchannels).sum(dim=(0, 2))
+    return like if return_complex else like.real
 
 
 class SEOBNRv4PHM:

@@ -163,6 +163,11 @@ int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t
  * lanes, 7 Hamiltonian with 32 lanes, 8 right-hand side with 32 lanes. */
 int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
                         cudaStream_t stream);
+/* warp-pair probes (no reference counterpart): which 0/1 = barrier round trip
+ * (suspending / spinning wait, out int[blocks * 4]), 2 = the pair right-hand
+ * side on binary 0 of `bins` (out double[blocks * 4]); threads a multiple of 64,
+ * at most 256 */
+int eob_pair_probe(const void *bins, int which, int iters, void *out, int blocks, int threads, cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Reference-shaped entry points (src/eob.pyx, src/dopr853.pyx, src/tdinterp.pyx)
@@ -227,6 +232,36 @@ int eob_dopr853_controller(unsigned char *flagSuccess, const double *err, double
  * upper_diag/diag/lower_diag as in the reference */
 int eob_interpolate_td(const double *t_arr, const double *propArrays, double *B, double *upper_diag, double *diag,
                        double *lower_diag, const int *lengths, int numBinAll, int nsubs, cudaStream_t stream);
+
+/* src/tdinterp.pyx:60 TDInterp_wrap2 -> src/interpolate.cu:441-549 (TD2): for binary b and sample
+ * i < lengths[b], t = dataTime[i], j = inds[max_length * b + i], x = t - ts[b * old_length + j];
+ * series s of binary b at propArrays/c1/c2/c3[b * (2K + 1) * old_length + s * old_lengths[b] + j]
+ * (s < K: Re h_k, K..2K-1: Im h_k, 2K: orbital phase); templateChannels[b * data_length + i]
+ * (complex, interleaved) = sum_k (Re + i Im) exp(-i m_k phi).  K <= 20.  Knot indices are
+ * clamped into the binary's rows. */
+int eob_tdinterp2(double *templateChannels, const double *dataTime, const double *ts, const double *propArrays,
+                  const double *c1, const double *c2, const double *c3, int old_length, const int *old_lengths,
+                  int data_length, int numBinAll, int numModes, const int *ls, const int *ms, const int *inds,
+                  const int *lengths, int max_length, cudaStream_t stream);
+/* src/tdinterp.pyx:40 TDInterp_wrap -> src/interpolate.cu:323-438 (TD): per-binary arrays given
+ * as HOST arrays of device addresses (templateChannels_ptrs, tsAll, propArraysAll, c1All, c2All,
+ * c3All, inds_ptrs) and HOST metadata (old_lengths, inds_start, ind_lengths), as the reference's
+ * host loop reads them; ls, ms and dataTime on the device.  Binary b writes
+ * templateChannels_b[data_length + i] for i < ind_lengths[b] from dataTime[inds_start[b] + i]. */
+int eob_tdinterp(const long long *templateChannels_ptrs, const double *dataTime, const long long *tsAll,
+                 const long long *propArraysAll, const long long *c1All, const long long *c2All,
+                 const long long *c3All, const int *old_lengths, int data_length, int numBinAll, int numModes,
+                 const int *ls, const int *ms, const long long *inds_ptrs, const int *inds_start,
+                 const int *ind_lengths, cudaStream_t stream);
+/* src/tdinterp.pyx:78 all_in_one_likelihood -> src/interpolate.cu:553-627: for frequency block
+ * q of 1024 bins, binary b and channel c, temp_sum[(q * num_bin_all + b) * nchannels + c]
+ * (complex, imaginary part 0) = sum_i |d_ci - (F+_cb h+_bi + Fx_cb hx_bi) exp(-2 pi i df i tau_cb)|^2
+ * / psd_ci, with data[c * data_length + i], psd[c * data_length + i], hp_fd/hc_fd[b * data_length
+ * + i] (complex), Fplus/Fcross/time_shift[c * num_bin_all + b].  The caller's lnL is
+ * -2 df sum over blocks and channels (eob/seobnrv4phm.py:806-809). */
+int eob_all_in_one_likelihood(double *temp_sum, const double *hp_fd, const double *hc_fd, const double *data,
+                              const double *psd, const double *Fplus, const double *Fcross, const double *time_shift,
+                              double df, int num_bin_all, int nchannels, int data_length, cudaStream_t stream);
 
 #ifdef __cplusplus
 }
