@@ -300,6 +300,39 @@ def run_plain(args, cfg, local):
                                                                "rows_max": int(ns.max().item())})}))
 
 
+OP_CENSUS = os.path.join(ROOT, "profiles", "tdinterp_fdlnl_fp64_census.md")
+
+
+def _op_flops(key):
+    """FP64 FLOP per output of a reference-shaped kernel, from the committed census."""
+    try:
+        with open(OP_CENSUS) as f:
+            for line in f:
+                if line.startswith(key):
+                    return float(line.split("=")[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def fp64_peak_tflops(lib, device):
+    """The device's FP64 issue peak, measured live (eob_fp64_probe: independent
+    DFMA chains on every lane), best of three."""
+    import torch
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    pk_out = torch.empty(nsm * 8 * 256, dtype=torch.float64, device=device)
+    iters = 4096
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.eob_fp64_probe(pk_out.data_ptr(), nsm * 8, 256, iters, torch.cuda.current_stream().cuda_stream)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * 8 * iters * nsm * 8 * 256 / (best / 1e3) / 1e12
+
+
 def run_op(args, local):
     """Reference-shaped kernels outside the fused path, timed alone on
     synthetic inputs of the benchmark's shapes (B = 1024 binaries, N = 2^17
@@ -340,8 +373,9 @@ def run_op(args, local):
             pytdinterp.TDInterp_wrap2(out, tgrid, ts, *arrs, L, old, N, B, K, ms, ms, inds, lengths, N)
         units = B * N
         byts = units * (16 + 4 + 8) + B * nsubs * L * 32 + B * L * 8
+        flops = _op_flops("FLOP_PER_OUTPUT_TDINTERP2_K5" if K == 5 else "FLOP_PER_OUTPUT_TDINTERP2_K1")
         work = f"{B} binaries x {N} samples, {K} mode(s): write 16 B, read index 4 B and time 8 B per sample, " \
-               f"spline tables once"
+               f"spline tables once; {flops} FP64 FLOP per sample (census)"
     else:
         nch, N = 3, 65537
         hp = torch.randn(B * N, dtype=torch.complex128, generator=g).to(device)
@@ -353,10 +387,11 @@ def run_op(args, local):
 
         def once():
             pytdinterp.all_in_one_likelihood(temp, hp, hc, data, psd, F[0], F[1], F[2] * 0.01, 0.125, B, nch, N)
-        units = B * N
-        byts = units * 32 + nch * N * 24 + temp.numel() * 16
+        units = B * N * nch
+        byts = B * N * 32 + nch * N * 24 + temp.numel() * 16
+        flops = _op_flops("FLOP_PER_OUTPUT_FD_LNL")
         work = f"{B} binaries x {N} bins x {nch} detectors: templates 32 B per (binary, bin) read once, " \
-               f"data and PSD per detector"
+               f"data and PSD per detector; {flops} FP64 FLOP per (binary, bin, detector) (census)"
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     for _ in range(args.warmup):
         once()
@@ -371,12 +406,18 @@ def run_op(args, local):
         torch.cuda.synchronize()
         ms_l.append(e0.elapsed_time(e1))
     t = float(np.median(ms_l))
-    achieved = byts / (t / 1e3) / 1e9
+    gbs = byts / (t / 1e3) / 1e9
+    from eobgpu_gb300 import _lib
+    pk = fp64_peak_tflops(_lib.load(), device)
+    roof = {"bound": "fp64", "achieved": None, "peak": pk, "unit": "TFLOP/s", "frac": None, "traffic": None,
+            "work": work, "peak_source": "measured live: FP64 DFMA probe (eob_fp64_probe), burst",
+            "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}}
+    if flops:
+        roof["achieved"] = flops * units / (t / 1e3) / 1e12
+        roof["frac"] = roof["achieved"] / pk
     print(json.dumps({"op": args.op, "metric": "outputs/s", "value": units / (t / 1e3), "unit": "outputs/s",
-                      "ms": t, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
-                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                                   "frac": achieved / hbm, "traffic": None, "work": work,
-                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+                      "ms": t, "steps": args.steps, "warmup": args.warmup, "dtype": "f64", "roofline": roof,
                       "l2": "flushed between timed launches (256 MiB write)"}))
 
 
@@ -384,10 +425,11 @@ def run_serving(args, ws, rank, local):
     """Configuration 4: a seeded Poisson trace of walker requests (1..512
     binaries each, 80 % from a ball around the injection, 20 % from the
     configuration-1 prior) replayed in wall-clock time through
-    LikelihoodServer.  The arrival rate is set from a calibration so that the
-    server is about 70 % busy.  Every rank replays its own trace."""
+    LikelihoodServer.  The server's capacity is measured first (the whole
+    trace queued at once); the arrival rate is then set so that the offered
+    load is 70 % of that capacity.  Every rank replays its own trace."""
     import torch
-    from eobgpu_gb300.serving import LikelihoodServer, calibrate_rate
+    from eobgpu_gb300.serving import LikelihoodServer
     cfg = workload.CONFIGS[1]
     device = torch.device(f"cuda:{local}")
     torch.cuda.set_device(device)
@@ -399,7 +441,11 @@ def run_serving(args, ws, rank, local):
     trace = workload.serving_trace(args.requests, 1.0, stream=rank)
     for _ in range(args.warmup):
         server.evaluate(trace.params[0])
-    rate = calibrate_rate(server, trace.params, busy=0.7)
+    # capacity: the same requests all queued at t = 0 (the server saturated)
+    sat = server.run_trace(np.zeros(len(trace.params)), trace.params)
+    capacity = sat["binaries"] / sat["wall_s"]
+    mean_size = float(np.mean([len(np.atleast_2d(p)) for p in trace.params]))
+    rate = 0.7 * capacity / mean_size  # requests/s for 70 % of capacity
     barrier(ws)
     results = []
     with ClockSampler(local) as clk:
@@ -419,7 +465,7 @@ def run_serving(args, ws, rank, local):
                 "data": "synthetic: seeded Poisson trace of walker requests, white noise + one injection at SNR 30",
                 "config": {"workload": "config 4: serving, continuous batching over concurrent slots",
                            "requests": args.requests, "request_size": [1, 512], "rate_hz": rate,
-                           "target_busy": 0.7, "classes_max_steps_batch_slots": classes,
+                           "offered_load": "70 % of the measured capacity", "classes_max_steps_batch_slots": classes,
                            "admission": "by estimated trajectory rows (chirp-time fit x3), re-run on overflow",
                            "requeued": int(sum(r["requeued"] for r in results)), "lanes_per_binary": lanes,
                            "max_steps": args.max_steps, "dt_s": cfg.dt, "n_samples": cfg.n_samples,
@@ -429,6 +475,9 @@ def run_serving(args, ws, rank, local):
                         "d2h_bytes_per_step": int(nbin / ws / args.steps * 12)},
                 "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
                 "slot_busy_fraction": float(np.mean([r["slot_busy_fraction"] for r in results])),
+                "capacity": {"value": capacity, "unit": "evals/s",
+                             "how": "the same requests all queued at t = 0 (saturated server)",
+                             "slot_busy_fraction": sat["slot_busy_fraction"]},
                 "batches": int(sum(r["batches"] for r in results)),
                 "gpu_launches": int(8 * sum(r["batches"] for r in results)),
                 "roofline": None, "cpu_baseline": None, "clocks": clocks, "status_ok": bool(ok)}
@@ -619,18 +668,7 @@ def main():
                 # (one FP64 warp instruction per 64 cycles at the sampled clock)
                 "fp64_slots_per_rhs_on_path": us_rhs * sm_mhz / 64.0}
     # FP64 peak of this device, measured
-    nsm = torch.cuda.get_device_properties(device).multi_processor_count
-    pk_out = torch.empty(nsm * 8 * 256, dtype=torch.float64, device=device)
-    iters = 4096
-    best = 1e30
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        wl.lib.eob_fp64_probe(pk_out.data_ptr(), nsm * 8, 256, iters, torch.cuda.current_stream().cuda_stream)
-        e1.record()
-        torch.cuda.synchronize()
-        best = min(best, e0.elapsed_time(e1))
-    fp64_peak = 2.0 * 8 * iters * nsm * 8 * 256 / (best / 1e3) / 1e12
+    fp64_peak = fp64_peak_tflops(wl.lib, device)
     roof = None
     if F_RHS:
         achieved = F_RHS * cnt["rhs_binaries"] / (stage_ms["integrate"] / 1e3) / 1e12
