@@ -232,7 +232,8 @@ def config_block(cfg, args, extra=None):
          "f0_hz": list(cfg.f0), "modes": [list(m) for m in cfg.modes], "dt_s": cfg.dt, "n_samples": cfg.n_samples,
          "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12, "queue": "longest first",
          "l2": "flushed between timed steps (256 MiB write)",
-         "lanes_per_binary": getattr(args, "lanes", 0) or "auto"}
+         "lanes_per_binary": getattr(args, "lanes", 0) or "auto",
+         "integrator_block": getattr(args, "block", 0) or "default", "integrator_grid": getattr(args, "grid", 0) or "auto"}
     if extra:
         d.update(extra)
     return d
@@ -505,6 +506,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="integrator lanes per binary (0: chosen from the batch size)")
+    ap.add_argument("--block", type=int, default=0, help="integrator threads per block (0: default)")
+    ap.add_argument("--grid", type=int, default=0, help="integrator blocks (0: one wave of resident blocks)")
     ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl"],
                     help="time one reference-shaped kernel alone (mode synthesis TD2, or FD likelihood partials)")
     ap.add_argument("--census", action="store_true",
@@ -546,6 +549,8 @@ def main():
     from eobgpu_gb300 import _lib
     opt = _lib.default_options()
     opt.lanes_per_binary = args.lanes
+    opt.block = args.block
+    opt.grid = args.grid
     mixed = args.config == 3 and not args.fp64
     opt.precision = 1 if mixed else 0
     P = torch.tensor(params, device=device)
