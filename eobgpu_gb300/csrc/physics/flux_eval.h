@@ -335,11 +335,14 @@ struct FluxLane {
     double vp[8];  // vphi^(2 e), e = 2..9
 };
 
-EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+// the shared pieces with log v given (a warp pair computes it as log(omega) / 3
+// on the other warp)
+EOB_HD FluxLane flux_lane_make_lv(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w,
+                                  double lv)
 {
     FluxLane f;
     f.v = v;
-    f.lv = eob_log(v);
+    f.lv = lv;
     const double v2 = v * v, v4 = v2 * v2;
     f.v12 = v4 * v4 * v4;
     const double vphi = omega / (w * w);
@@ -356,6 +359,11 @@ EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, do
     f.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
     f.Sodd = v * pphi;
     return f;
+}
+
+EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+{
+    return flux_lane_make_lv(t, pphi, omega, Hreal, v, w, eob_log(v));
 }
 
 // m x / (1 - e^{-m x}) and 4 k^2 = 4 (m H omega)^2 for one m

@@ -13,8 +13,8 @@
 //   jets         log r, the log(r) parts          sqrt(u), the polynomial and
 //                                                 sqrt(u) parts (halves of the warp)
 //   combination  A(u), c(u)  -> even part         B_np, q  -> odd part
-//   flux         v = omega^(1/3), log v, v_phi    m factors (m x/(1-e^{-m x}), 4k^2),
-//                powers; multipoles 0..31         y_2/y_3, 1/(8 pi nu); multipoles 32..34
+//   flux         v = omega^(1/3), v_phi powers;   m factors (m x/(1-e^{-m x}), 4k^2),
+//                multipoles 0..31                 log v, y_2/y_3, 1/(8 pi nu); multipoles 32..34
 //
 // Values cross between the warps through shared memory at five pair
 // barriers per right-hand side (an mbarrier of 64 arrivals, waited on with a
@@ -40,7 +40,7 @@ struct PairXchg {
     double ev[4][32];      // role 0 -> both: even part of H_eff and its derivatives
     double od[4][32];      // role 1 -> both: odd part
     double T[8], k4[8];    // role 1 -> 0: m factors, m = 1..8
-    double fl[13];         // role 0 -> 1: v, log v, v^12, S_even, S_odd, v_phi^(2e) e = 2..9
+    double fl[13];         // v, log v (role 1 -> 0), v^12, S_even, S_odd, v_phi^(2e) e = 2..9 (role 0 -> 1)
     double part[2];        // flux partial sums of the two warps
     double aux[2];         // role 1 -> both: y_2 / y_3, 1 / (8 pi nu)
     unsigned long long slot;
@@ -227,17 +227,17 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction stream
         const double cr = cbrt((lane & 1) ? omega_c : omega);
         const double v = __shfl_sync(0xffffffffu, cr, 0), w = __shfl_sync(0xffffffffu, cr, 1);
-        const FluxLane f = flux_lane_make(t, L, omega, Hreal, v, w);
+        FluxLane f = flux_lane_make_lv(t, L, omega, Hreal, v, w, 0.0);
         if (lane == 0) {
             x.fl[0] = f.v;
-            x.fl[1] = f.lv;
             x.fl[2] = f.v12;
             x.fl[3] = f.Se;
             x.fl[4] = f.Sodd;
 #pragma unroll
             for (int q = 0; q < 8; ++q) x.fl[5 + q] = f.vp[q];
         }
-        pair_sync(ps);  // 4: FluxLane and m factors
+        pair_sync(ps);  // 4: FluxLane, log v and m factors
+        f.lv = x.fl[1];
         part = flux_warp_modes<0>(t, f, x, lane);
     } else {
         double Tm, k4m;
@@ -246,6 +246,10 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
             x.T[lane] = Tm;
             x.k4[lane] = k4m;
         }
+        // log v = log(omega) / 3, here rather than after the cube root on the
+        // other warp, whose flux set-up is the longer of the two
+        const double lv = eob_log(omega) * (1.0 / 3.0);
+        if (lane == 0) x.fl[1] = lv;
         pair_sync(ps);  // 4
         FluxLane f;
         f.v = x.fl[0];
