@@ -13,8 +13,9 @@
 //   jets         log r, the log(r) parts          sqrt(u), the polynomial and
 //                                                 sqrt(u) parts (halves of the warp)
 //   combination  A(u), c(u)  -> even part         B_np, q  -> odd part
-//   flux         v = omega^(1/3), v_phi powers;   m factors (m x/(1-e^{-m x}), 4k^2),
-//                multipoles 0..31                 log v, y_2/y_3, 1/(8 pi nu); multipoles 32..34
+//   H, flux      H and its gradient;              m factors (m x/(1-e^{-m x}), 4k^2),
+//                v = omega^(1/3), v_phi powers;   log v, y_2/y_3, 1/(8 pi nu); multipoles 32..34
+//                multipoles 0..31
 //
 // Values cross between the warps through shared memory at five pair
 // barriers per right-hand side (an mbarrier of 64 arrivals, waited on with a
@@ -43,6 +44,7 @@ struct PairXchg {
     double fl[13];         // v, log v (role 1 -> 0), v^12, S_even, S_odd, v_phi^(2e) e = 2..9 (role 0 -> 1)
     double part[2];        // flux partial sums of the two warps
     double aux[2];         // role 1 -> both: y_2 / y_3, 1 / (8 pi nu)
+    double ham[3];         // role 0 -> both: dH/dr, dH/dp_r, dH/dL at the state
     unsigned long long slot;
 };
 
@@ -214,16 +216,18 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
     od.du = x.od[1][lane];
     od.dp = x.od[2][lane];
     od.dL = x.od[3][lane];
-    const HamPart hp = comb_final(J, u, ev, od);
-    const double Hreal = __shfl_sync(0xffffffffu, hp.Hreal, 0);
-    const double dHdr = __shfl_sync(0xffffffffu, hp.dHdr, 0);
-    const double dHdpr = __shfl_sync(0xffffffffu, hp.dHdpr, 0);
-    const double omega = __shfl_sync(0xffffffffu, hp.dHdL, 0);
-    const double omega_c = __shfl_sync(0xffffffffu, hp.dHdL, 1);
-
-    // ---- flux
+    // ---- H and the flux set-up
     double part;
     if (role == 0) {
+        const HamPart hp = comb_final(J, u, ev, od);
+        const double Hreal = __shfl_sync(0xffffffffu, hp.Hreal, 0);
+        const double omega = __shfl_sync(0xffffffffu, hp.dHdL, 0);
+        const double omega_c = __shfl_sync(0xffffffffu, hp.dHdL, 1);
+        if (lane == 0) {
+            x.ham[0] = hp.dHdr;
+            x.ham[1] = hp.dHdpr;
+            x.ham[2] = hp.dHdL;
+        }
         // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction stream
         const double cr = cbrt((lane & 1) ? omega_c : omega);
         const double v = __shfl_sync(0xffffffffu, cr, 0), w = __shfl_sync(0xffffffffu, cr, 1);
@@ -240,14 +244,22 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         f.lv = x.fl[1];
         part = flux_warp_modes<0>(t, f, x, lane);
     } else {
+        // this warp needs H_real omega and omega, not the whole combination:
+        // with D = dH_eff/dL, H_real omega = M^2 D exactly (H_real = M s,
+        // omega = M D / s), and omega = M D / s with s from the same square root
+        const double D = x.ev[3][0] + x.od[3][0];
+        const double hw = (J.M * J.M) * D;
         double Tm, k4m;
-        flux_m_factors((lane & 7) + 1, 4.0 * kPi * Hreal * omega, Hreal * omega, &Tm, &k4m);
+        flux_m_factors((lane & 7) + 1, 4.0 * kPi * hw, hw, &Tm, &k4m);
         if (lane < 8) {
             x.T[lane] = Tm;
             x.k4[lane] = k4m;
         }
         // log v = log(omega) / 3, here rather than after the cube root on the
         // other warp, whose flux set-up is the longer of the two
+        const double heff = x.ev[0][0] + x.od[0][0];
+        const double s2 = fma(2.0 * J.nu, heff - 1.0, 1.0);
+        const double omega = J.M * eob_rsqrt(s2) * D;
         const double lv = eob_log(omega) * (1.0 / 3.0);
         if (lane == 0) x.fl[1] = lv;
         pair_sync(ps);  // 4
@@ -266,6 +278,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
     if (lane == 0) x.part[role] = part;
     pair_sync(ps);  // 5: flux partial sums
     const double total = x.part[0] + x.part[1];
+    const double dHdr = x.ham[0], dHdpr = x.ham[1], omega = x.ham[2];
     // F / omega with F = total omega^2 / (8 pi) / nu
     const double fo = total * omega * x.aux[1];
     k[0] = dHdpr;
