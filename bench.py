@@ -497,8 +497,11 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--fp64", action="store_true", help="configuration 3 in FP64 instead of mixed precision")
     ap.add_argument("--requests", type=int, default=2000, help="configuration 4: requests in the trace")
-    ap.add_argument("--head", type=int, default=-1,
-                    help="configuration 5: longest binaries run concurrently with 8 lanes each (-1: B/50)")
+    ap.add_argument("--head", type=int, default=0,
+                    help="configuration 5: longest binaries run concurrently on their own workspace (-1: B/50)")
+    ap.add_argument("--slots", type=int, default=1, help="configuration 5: concurrent chunk workspaces")
+    ap.add_argument("--hbm-frac", type=float, default=0.9, help="configuration 5: HBM budget, fraction of free memory")
+    ap.add_argument("--head-lanes", type=int, default=8, help="configuration 5: lanes per binary of the head")
     ap.add_argument("--no-graph", action="store_true", help="launch the path eagerly instead of replaying a CUDA graph")
     ap.add_argument("--autotune", action="store_true", help="pick lanes per binary, block and spline tile by timing")
     ap.add_argument("--batch", type=int, default=0)
@@ -562,8 +565,10 @@ def main():
     if args.config == 5:
         from eobgpu_gb300.pipeline import ChunkedLikelihood
         head = args.head if args.head >= 0 else B // 50
-        chunked = ChunkedLikelihood(B, cfg.n_samples, list(cfg.modes), args.max_steps, slots=2, options=opt,
-                                    head=head, head_lanes=8, device=device)
+        free, _ = torch.cuda.mem_get_info(device)
+        chunked = ChunkedLikelihood(B, cfg.n_samples, list(cfg.modes), args.max_steps, slots=args.slots, options=opt,
+                                    head=head, head_lanes=args.head_lanes, device=device,
+                                    hbm_budget_bytes=int(args.hbm_frac * free))
         wl = chunked.engines[0]
 
         def run_any(Pd, Od):

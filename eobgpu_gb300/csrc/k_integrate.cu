@@ -539,10 +539,14 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, 0);
         if (per_sm < 1) per_sm = 1;
-        // lane groups: at most one warp per SM sub-partition, so that a long
-        // binary's group never shares the FP64 pipe; later binaries wait in
-        // the queue instead (it hands out the longest first)
-        if (G > 1) {
+        // at most one warp per SM sub-partition, so that no binary's chain
+        // shares an FP64 pipe (a warp alone on a sub-partition keeps its FP64
+        // pipe ~80 % busy); later binaries wait in the queue instead, which
+        // hands out the longest first.  With three warps per sub-partition a
+        // ragged batch's longest binaries run three times slower (65 536
+        // one-lane binaries: 22 s in chunks at three warps, 11 s in one launch
+        // at one warp)
+        {
             const int cap = (4 * 32 + bs - 1) / bs;
             if (per_sm > cap) per_sm = cap;
         }

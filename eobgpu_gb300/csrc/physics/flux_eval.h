@@ -335,9 +335,9 @@ struct FluxLane {
     double vp[8];  // vphi^(2 e), e = 2..9
 };
 
-// the shared pieces with log v given (a warp pair computes it as log(omega) / 3
-// on the other warp)
-EOB_HD FluxLane flux_lane_make_lv(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w,
+// the shared pieces from v and v_phi = omega / omega_c^(2/3), with log v
+// given (a warp pair computes it as log(omega) / 3 on the other warp)
+EOB_HD FluxLane flux_lane_make_rv(const FluxTable &t, double pphi, double omega, double Hreal, double v, double vphi,
                                   double lv)
 {
     FluxLane f;
@@ -345,7 +345,6 @@ EOB_HD FluxLane flux_lane_make_lv(const FluxTable &t, double pphi, double omega,
     f.lv = lv;
     const double v2 = v * v, v4 = v2 * v2;
     f.v12 = v4 * v4 * v4;
-    const double vphi = omega / (w * w);
     const double p1 = vphi * vphi;
     const double p2 = p1 * p1, p3 = p2 * p1, p4 = p2 * p2;
     f.vp[0] = p2;
@@ -359,6 +358,12 @@ EOB_HD FluxLane flux_lane_make_lv(const FluxTable &t, double pphi, double omega,
     f.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
     f.Sodd = v * pphi;
     return f;
+}
+
+EOB_HD FluxLane flux_lane_make_lv(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w,
+                                  double lv)
+{
+    return flux_lane_make_rv(t, pphi, omega, Hreal, v, omega / (w * w), lv);
 }
 
 EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)

@@ -228,10 +228,12 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
             x.ham[1] = hp.dHdpr;
             x.ham[2] = hp.dHdL;
         }
-        // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction stream
-        const double cr = cbrt((lane & 1) ? omega_c : omega);
-        const double v = __shfl_sync(0xffffffffu, cr, 0), w = __shfl_sync(0xffffffffu, cr, 1);
-        FluxLane f = flux_lane_make_lv(t, L, omega, Hreal, v, w, 0.0);
+        // reciprocal cube roots of omega (even lanes) and omega_c (odd lanes)
+        // in one instruction stream: v = omega r_omega^2 and
+        // v_phi = omega / omega_c^(2/3) = omega r_c^2 without a division
+        const double rc = rcbrt((lane & 1) ? omega_c : omega);
+        const double r0 = __shfl_sync(0xffffffffu, rc, 0), r1 = __shfl_sync(0xffffffffu, rc, 1);
+        FluxLane f = flux_lane_make_rv(t, L, omega, Hreal, omega * (r0 * r0), omega * (r1 * r1), 0.0);
         if (lane == 0) {
             x.fl[0] = f.v;
             x.fl[2] = f.v12;

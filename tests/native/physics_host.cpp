@@ -78,7 +78,8 @@ void phys_ham_pair(const double *st, const double *add, int n, double *out)
 // cube roots
 static double flux_pair_host(const eob::FluxTable &t, double pphi, double omega, double Hreal, double omega_c)
 {
-    const eob::FluxLane f = eob::flux_lane_make_lv(t, pphi, omega, Hreal, cbrt(omega), cbrt(omega_c),
+    const double r0 = 1.0 / cbrt(omega), r1 = 1.0 / cbrt(omega_c);
+    const eob::FluxLane f = eob::flux_lane_make_rv(t, pphi, omega, Hreal, omega * (r0 * r0), omega * (r1 * r1),
                                                    eob::eob_log(omega) * (1.0 / 3.0));
     double T[8], k4[8];
     for (int m = 1; m <= 8; ++m)
