@@ -39,6 +39,8 @@ struct FluxTable {
     EOB_HD double c_eta() const { return eta; }
     EOB_HD double c_equal() const { return equal_mass; }
     EOB_HD double c_h22() const { return h22calib; }
+    EOB_HD double c_gmul(int i, int, int) const { return gmul[i]; }
+    EOB_HD double c_inv2eta() const { return inv2eta; }
 };
 
 // The same flux inputs read straight from a FacCoeffs table and
@@ -64,6 +66,13 @@ struct FacFluxView {
     EOB_HD double c_eta() const { return eta; }
     EOB_HD double c_equal() const { return equal_mass; }
     EOB_HD double c_h22() const { return h22; }
+    EOB_HD double c_gmul(int i, int l, int m) const
+    {
+        double f = 1.0;
+        for (int j = 2; j <= l; ++j) f *= (double)j;
+        return (double)(m * m) * c_nabs2(i, l, m) / (f * f);
+    }
+    EOB_HD double c_inv2eta() const { return 0.5 / eta; }
 };
 
 EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *prefix_re, const double *prefix_im,
@@ -104,34 +113,47 @@ EOB_HD constexpr double fact2_sq(int l)
 
 struct FluxShared {
     double v, lv, vphi2, Se, Sodd, x, omega, E1;
+    double v12, S2e, S2o;  // v^12, S_even^2, S_odd^2 (one-lane flux)
 };
 
-// contribution m^2 |h_lm|^2 / (omega^2) of one (l, m); P = prod_{j<=l} (4k^2 + j^2)
+// x^N for a compile-time N >= 1 by squaring
+template <int N>
+EOB_HD double ipow(double x)
+{
+    if constexpr (N == 1) return x;
+    else if constexpr (N % 2 == 0) {
+        const double h = ipow<N / 2>(x);
+        return h * h;
+    } else {
+        return x * ipow<N - 1>(x);
+    }
+}
+
+// contribution m^2 |h_lm|^2 / (omega^2) of one (l, m); TP = (m x)/(1 - e^{-m x})
+// prod_{j<=l} (4k^2 + j^2).  rho_lm by fma Horner, rho^l by squaring, the
+// constant m^2 |h^N_lm|^2 / (l!)^2 from the table, S^2 once per parity.
 template <int l, int m, class Tab>
-EOB_HD double flux_term(const Tab &t, const FluxShared &s, double Tpre, double P, const double *vp2)
+EOB_HD double flux_term(const Tab &t, const FluxShared &s, double TP, const double *vp2)
 {
     constexpr int i = (l - 2) * (l + 1) / 2 + (m - 1);
     constexpr int eps = (l + m) % 2;
     constexpr int kmax = (l == 2) ? 10 : (l == 3) ? 8 : (l == 4) ? 6 : (l == 5) ? ((m == 5) ? 6 : (m == 3 || m == 1) ? 5 : 4)
                                    : (l == 6) ? ((m % 2 == 0) ? 4 : 3) : (l == 7) ? ((m % 2 == 1) ? 3 : 2) : 2;
     constexpr bool has_log = (l <= 4);
-    // eulerlog_m = gamma + log(2 m v)
+    // eulerlog_m = gamma + log(2 m v); c_k = rho_k + rhol_k eulerlog_m
     const double elm = t.c_elog(m) + s.lv;
-    double rho = 0.0;
+    auto ck = [&](int k) {
+        double c = t.c_rho(i, k);
+        if (has_log && (k == 6 || k == 7 || k == 8 || k == 10)) c = fma(t.c_rhol(i, k), elm, c);
+        return c;
+    };
+    // rho = 1 + v (c_1 + v (c_2 + ... + v c_kmax))
+    double acc = ck(kmax);
 #pragma unroll
-    for (int k = kmax; k >= 1; --k) {
-        double ck = t.c_rho(i, k);
-        if (has_log && (k == 6 || k == 7 || k == 8 || k == 10)) ck = fma(t.c_rhol(i, k), elm, ck);
-        rho = (rho + ck) * s.v;
-    }
-    rho += 1.0;
-    if (l == 2 && m == 2) {
-        const double v4 = (s.v * s.v) * (s.v * s.v);
-        rho = fma(t.c_h22(), v4 * v4 * v4, rho);
-    }
-    double rpl = rho;
-#pragma unroll
-    for (int q = 1; q < l; ++q) rpl *= rho;
+    for (int k = kmax - 1; k >= 1; --k) acc = fma(acc, s.v, ck(k));
+    double rho = fma(acc, s.v, 1.0);
+    if (l == 2 && m == 2) rho = fma(t.c_h22(), s.v12, rho);
+    double rpl = ipow<l>(rho);
     const bool has_f = (l == 2 && m == 1) || (l == 3 && (m == 3 || m == 1)) || (l == 4 && (m == 3 || m == 1));
     if (has_f) {
         const double v2 = s.v * s.v;
@@ -140,10 +162,8 @@ EOB_HD double flux_term(const Tab &t, const FluxShared &s, double Tpre, double P
     } else if (m % 2 == 1) {
         rpl = (t.c_equal() != 0.0) ? 0.0 : rpl;
     }
-    const double S = eps ? s.Sodd : s.Se;
-    const double hn2 = t.c_nabs2(i, l, m) * vp2[l + eps];
-    const double T2 = Tpre * P * (1.0 / fact2_sq(l));
-    return (double)(m * m) * T2 * (S * S) * (rpl * rpl) * hn2;
+    const double S2 = eps ? s.S2o : s.S2e;
+    return t.c_gmul(i, l, m) * TP * S2 * (rpl * rpl) * vp2[l + eps];
 }
 
 // Accumulate all l for one m (products over j carried across l).
@@ -152,7 +172,7 @@ EOB_HD double flux_m_l(const Tab &t, const FluxShared &s, double Tpre, double P,
 {
     P *= k2x4 + (double)(l * l);
     double here = 0.0;
-    if constexpr (l >= (m > 2 ? m : 2)) here = flux_term<l, m, Tab>(t, s, Tpre, P, vp2);
+    if constexpr (l >= (m > 2 ? m : 2)) here = flux_term<l, m, Tab>(t, s, Tpre * P, vp2);
     if constexpr (l < kLMax) return here + flux_m_l<m, l + 1, Tab>(t, s, Tpre, P, k2x4, vp2);
     else return here;
 }
@@ -176,11 +196,17 @@ EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, doubl
     s.omega = omega;
     s.v = cbrt(omega);
     s.lv = eob_log(s.v);
-    const double vphi_in = 1.0 / (omega_c * omega_c * r * r * r);
-    const double vphi = r * cbrt(vphi_in) * omega;
+    // v_phi = r (omega_c^2 r^3)^(-1/3) omega = omega omega_c^(-2/3)
+    (void)r;
+    const double rc = eob_rcbrt(omega_c);
+    const double vphi = omega * (rc * rc);
     s.vphi2 = vphi * vphi;
-    s.Se = (Hreal * Hreal - 1.0) / (2.0 * t.c_eta()) + 1.0;
+    s.Se = fma(Hreal * Hreal - 1.0, t.c_inv2eta(), 1.0);
     s.Sodd = s.v * pphi;
+    const double v2 = s.v * s.v, v4 = v2 * v2;
+    s.v12 = v4 * v4 * v4;
+    s.S2e = s.Se * s.Se;
+    s.S2o = s.Sodd * s.Sodd;
     s.x = 4.0 * kPi * Hreal * omega;
     double vp2[10];
     vp2[0] = 1.0;

@@ -5,13 +5,34 @@
 // (src/EOB.cu:139-222, grad_Ham_align_AD_single) and its second gradient
 // evaluation at p_r = 0 (src/EOB.cu:2611-2616).  Every function of r is
 // carried as a jet (value, d/du) in u = 1/r; the only transcendental calls
-// are one log (eob_log, fastlog.h), two square roots, a reciprocal and the final square roots.
+// are one log (eob_log, fastlog.h), a square root, reciprocals and reciprocal square roots.
 // No pow() anywhere: on GB300 one FP64 pow costs about 100 DFMA slots.
 #pragma once
 #include "ham_coeffs.h"
 #include "fastlog.h"
 
 namespace eob {
+
+// 1/sqrt(x): the device's reciprocal square root (one instruction sequence
+// instead of a square root and a division); on the host 1/sqrt(x)
+EOB_HD double eob_rsqrt(double x)
+{
+#ifdef __CUDA_ARCH__
+    return rsqrt(x);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
+// x^(-1/3): the device's reciprocal cube root; on the host 1/cbrt(x)
+EOB_HD double eob_rcbrt(double x)
+{
+#ifdef __CUDA_ARCH__
+    return rcbrt(x);
+#else
+    return 1.0 / cbrt(x);
+#endif
+}
 
 struct HamEval {
     double H;        // H_real / nu  (reference evaluate_Ham_align_AD)
@@ -104,8 +125,9 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
     const double WL = 2.0 * L * cu.v;
 
     const double AW = A.v * W;
-    const double heven = sqrt(AW);
-    const double ih2 = 0.5 / heven;
+    const double rAW = eob_rsqrt(AW);
+    const double heven = AW * rAW;
+    const double ih2 = 0.5 * rAW;
     const double hev_u = (A.d * W + A.v * Wu) * ih2;
     const double hev_p = A.v * Wp * ih2;
     const double hev_L = A.v * WL * ih2;
@@ -131,9 +153,11 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
 
     const double heff = heven + hodd;
     const double nu = h.nu, M = h.M;
-    const double s = sqrt(1.0 + 2.0 * nu * (heff - 1.0));
+    const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
+    const double rs = eob_rsqrt(s2);
+    const double s = s2 * rs;
     const double H = M * s / nu;
-    const double f = M / s;  // M^2 / (nu H)
+    const double f = M * rs;  // M^2 / (nu H)
     out->H = H;
     out->Hreal = M * s;
     out->dHdr = -u2 * f * (hev_u + hodd_u);
@@ -142,10 +166,11 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
 
     // circular frequency: dH/dL at p_r = 0
     const double W0 = 1.0 + L2 * cu.v;
-    const double hev0 = sqrt(A.v * W0);
+    const double AW0 = A.v * W0;
+    const double r0 = eob_rsqrt(AW0);
     const double hodd0 = L * u3i * n0.v;
-    const double s0 = sqrt(1.0 + 2.0 * nu * (hev0 + hodd0 - 1.0));
-    out->omega_c = (M / s0) * (A.v * L * cu.v / hev0 + u3i * n0.v);
+    const double rs0 = eob_rsqrt(fma(2.0 * nu, fma(AW0, r0, hodd0) - 1.0, 1.0));
+    out->omega_c = (M * rs0) * fma(A.v * L * cu.v, r0, u3i * n0.v);
 }
 
 }  // namespace eob

@@ -40,17 +40,6 @@ enum JetId : int {
     J_N3,
 };
 
-// 1/sqrt(x): the device's reciprocal square root (one instruction sequence
-// instead of a square root and a division); on the host 1/sqrt(x)
-EOB_HD double eob_rsqrt(double x)
-{
-#ifdef __CUDA_ARCH__
-    return rsqrt(x);
-#else
-    return 1.0 / sqrt(x);
-#endif
-}
-
 struct HamJets {
     double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
     double n4, apsq, nu, M;
