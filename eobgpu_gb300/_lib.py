@@ -21,7 +21,8 @@ c_ll = ctypes.c_longlong
 class EobOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("h_init", c_double), ("step_back", c_double),
                 ("fine_step", c_double), ("ic_mode", c_int), ("precision", c_int), ("block", c_int),
-                ("grid", c_int), ("max_tries", c_ll), ("lanes_per_binary", c_int), ("spline_tile", c_int)]
+                ("grid", c_int), ("max_tries", c_ll), ("lanes_per_binary", c_int), ("spline_tile", c_int),
+                ("head_quads", c_int)]
 
 
 class EobViews(ctypes.Structure):

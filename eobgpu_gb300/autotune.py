@@ -63,7 +63,7 @@ def _time(wl, P, D, dt, amp, order, reps):
 
 
 def tune(params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, modes=((2, 2),), max_steps: int = 6000,
-         lanes=(1, 2, 4, 8, 16, 32, 64), blocks=(64, 128, 256), spline_tiles=(1, 4), reps: int = 1,
+         lanes=(1, 2, 4, 8, 16, 32, 64, 128), blocks=(64, 128, 256), spline_tiles=(1, 4), reps: int = 1,
          cache_file: str | None = None, base: _lib.EobOptions | None = None) -> TuneResult:
     """Time every candidate on this batch and return the fastest.  The lanes
     per binary are searched first (block 128); the block size only for the

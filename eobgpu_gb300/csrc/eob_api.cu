@@ -22,6 +22,7 @@ void eob_options_default(eob_options *o)
     o->max_tries = 0;
     o->lanes_per_binary = 0;
     o->spline_tile = 0;
+    o->head_quads = -1;
 }
 
 size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples)

@@ -27,6 +27,7 @@
 // non-finite error estimate or step, or at the row capacity.
 #include "eob_device.cuh"
 #include "rhs_pair.cuh"
+#include "rhs_quad.cuh"
 
 namespace eob {
 namespace dp {
@@ -124,6 +125,8 @@ struct IntArgs {
     int *status;
     int *rhs;
     unsigned long long *queue;
+    unsigned long long *qslot;  // the work-queue counter (queue[0], or queue[7] for a head of four-warp groups)
+    int base;                   // first entry of `order` this queue hands out
     double rtol, atol, h_init, fine_step, step_back, tmax;
     long long max_tries;
 };
@@ -134,8 +137,8 @@ __device__ __forceinline__ double pick4(const double v[4], int q)
     return q == 0 ? v[0] : (q == 1 ? v[1] : (q == 2 ? v[2] : v[3]));
 }
 
-template <int G>
-__device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_all, unsigned long long *bars)
+template <int G, class X = PairXchg>
+__device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, unsigned long long *bars)
 {
     // G consecutive lanes carry one binary; every lane of the group keeps the
     // same control state, the Hamiltonian jets and flux multipoles are split
@@ -151,25 +154,27 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
     // adds the four components in the reference's order, so every lane
     // reaches the same accept/reject decision with the same bits.
     //
-    // G = 64: a warp pair per binary (rhs_pair.cuh); each warp runs the
-    // control state of a 32-lane group, role 0 writes the results.
-    constexpr bool kPair = (G == 64);
+    // G = 64 / 128: two / four warps per binary (rhs_pair.cuh, rhs_quad.cuh);
+    // each warp runs the control state of a 32-lane group, role 0 writes the
+    // results.
+    constexpr bool kPair = (G >= 64);
+    constexpr int NW = G / 32;          // warps per binary (groups of several warps)
     constexpr int GW = kPair ? 32 : G;  // lanes of the group inside one warp
     constexpr bool kDist = (G >= 4);
     constexpr int NC = kDist ? 1 : 4;  // state components held by one lane
     const int lane = threadIdx.x & 31;
     const int sub = lane & (GW - 1);
-    const int role = kPair ? (int)((threadIdx.x >> 5) & 1) : 0;
+    const int role = kPair ? (int)((threadIdx.x >> 5) % NW) : 0;
     const int cq = kDist ? (sub & 3) : 0;  // the component a distributing lane holds
     const bool leader = (sub == 0) && role == 0;
     const bool writer = kDist ? (sub < 4 && role == 0) : leader;  // writes trajectory components
     const unsigned gmask = (GW == 32) ? 0xffffffffu : (((1u << GW) - 1u) << (lane - sub));
-    PairXchg *xch = nullptr;
+    X *xch = nullptr;
     PairSync ps{0u, 0u, true};
     if constexpr (kPair) {
-        const int pair = (int)(threadIdx.x >> 6);
-        xch = &xch_all[pair];
-        ps.bar = (unsigned)__cvta_generic_to_shared(&bars[pair]);
+        const int grp = (int)(threadIdx.x / G);
+        xch = &xch_all[grp];
+        ps.bar = (unsigned)__cvta_generic_to_shared(&bars[grp]);
     }
     // per-lane DOPR853 state (components comp(c) = kDist ? cq : c)
     double k[11][NC];  // slopes k1..k10 (slot 0 unused)
@@ -195,7 +200,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
         // ------------------------------------------------ bookkeeping
         if (phase == kIdle && !queue_empty) {
             unsigned long long slot = 0;
-            if (leader) slot = atomicAdd(&a.queue[0], 1ull);
+            if (leader) slot = atomicAdd(a.qslot, 1ull);
             if constexpr (kPair) {
                 if (leader) xch->slot = slot;
                 pair_sync(ps);
@@ -205,7 +210,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
                     // the partner warp stopped answering: record the binary
                     // this warp took (if any) and leave
                     if (leader && got < (unsigned long long)a.B) {
-                        const int bb = a.order ? a.order[got] : (int)got;
+                        const int bb = a.order ? a.order[a.base + (int)got] : a.base + (int)got;
                         a.nsteps[bb] = 1;
                         a.status[bb] |= EOB_ST_SYNC | EOB_ST_SHORT;
                     }
@@ -217,7 +222,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
             if (slot >= (unsigned long long)a.B) {
                 queue_empty = true;
             } else {
-                b = a.order ? a.order[slot] : (int)slot;
+                b = a.order ? a.order[a.base + (int)slot] : a.base + (int)slot;
                 rec = &a.bins[b];
                 tr = a.traj + (size_t)b * (size_t)a.cap * kTrajStride;
                 st = 0;
@@ -271,7 +276,8 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
         // ------------------------------------------------ the one RHS per loop
         double kk[4];
         if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
-        else if constexpr (kPair) eob_rhs_pair(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
+        else if constexpr (G == 64) eob_rhs_pair(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
+        else if constexpr (G == 128) eob_rhs_quad(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
         else eob_rhs_group<G>(rec->jets, rec->flux, arg, kk, sub);
         if constexpr (kPair) {
             if (!ps.ok) {
@@ -501,13 +507,13 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, PairXchg *xch_a
 template <int G>
 __global__ void __launch_bounds__(256, 1) k_integrate(IntArgs a)
 {
-    integrate_body<G>(a, nullptr, nullptr);
+    integrate_body<G>(a, (PairXchg *)nullptr, nullptr);
 }
 
 template <int G>
 __global__ void __launch_bounds__(256) k_integrate_lane(IntArgs a)
 {
-    integrate_body<G>(a, nullptr, nullptr);
+    integrate_body<G>(a, (PairXchg *)nullptr, nullptr);
 }
 
 // warp pairs: blockDim.x a multiple of 64, at most kPairMax pairs
@@ -519,13 +525,54 @@ __global__ void __launch_bounds__(256, 1) k_integrate_pair(IntArgs a)
     integrate_body<64>(a, xch, bars);
 }
 
+// The longest binaries on four warps, the rest on warp pairs, in one launch
+// of 128-thread blocks: blocks [0, nq) first run four-warp groups over the
+// first `head` binaries of the order (their own queue counter, queue[7]),
+// then join the other blocks as two pairs over the remaining binaries.
+__global__ void __launch_bounds__(128, 1) k_integrate_mixed(IntArgs a, int nq, int head)
+{
+    __shared__ QuadXchg xq;
+    __shared__ PairXchg xp[2];
+    __shared__ unsigned long long bq[1], bp[2];
+    if (threadIdx.x == 0) {
+        const unsigned aq = (unsigned)__cvta_generic_to_shared(&bq[0]);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(aq), "r"(128) : "memory");
+        for (int p = 0; p < 2; ++p) {
+            const unsigned ap = (unsigned)__cvta_generic_to_shared(&bp[p]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(ap), "r"(64) : "memory");
+        }
+    }
+    __syncthreads();
+    if ((int)blockIdx.x < nq) {
+        IntArgs aq = a;
+        aq.B = head;
+        aq.qslot = &a.queue[7];
+        integrate_body<128, QuadXchg>(aq, &xq, bq);
+        __syncthreads();  // the block leaves the four-warp queue together
+    }
+    IntArgs ap = a;
+    ap.base = a.base + head;
+    ap.B = a.B - head;
+    integrate_body<64>(ap, xp, bp);
+}
+
+// warp quads: blockDim.x a multiple of 128, at most kQuadMax quads
+__global__ void __launch_bounds__(256, 1) k_integrate_quad(IntArgs a)
+{
+    __shared__ QuadXchg xch[kQuadMax];
+    __shared__ unsigned long long bars[kQuadMax];
+    group_init(bars, (int)(blockDim.x / 128), 128);
+    integrate_body<128, QuadXchg>(a, xch, bars);
+}
+
 template <int G>
 cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
 {
     // little or no shared memory: give the SM's unified L1/shared storage to
     // L1, where the lanes' coefficient tables and slope arrays live
     void (*kern)(IntArgs);
-    if constexpr (G == 64) kern = k_integrate_pair;
+    if constexpr (G == 128) kern = k_integrate_quad;
+    else if constexpr (G == 64) kern = k_integrate_pair;
     else if constexpr (G >= 4) kern = k_integrate<G>;
     else kern = k_integrate_lane<G>;
     static bool carveout_set = false;
@@ -604,9 +651,33 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
     a.max_tries = ra.opt.max_tries > 0 ? ra.opt.max_tries : 2LL * w.L.Lc + 100;
     const int bs = (ra.opt.block > 0 && ra.opt.block <= 256 && ra.opt.block % 32 == 0) ? ra.opt.block : 128;
     int G = ra.opt.lanes_per_binary;
-    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32 && G != 64) G = auto_lanes_per_binary(ra.B);
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32 && G != 64 && G != 128)
+        G = auto_lanes_per_binary(ra.B);
+    a.qslot = &w.queue[0];
+    a.base = 0;
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long) * 8, s);
     if (e != cudaSuccess) return e;
+    // warp pairs with a head on four warps
+    if (G == 64 && ra.opt.head_quads != 0) {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        int head = ra.opt.head_quads;
+        if (head < 0) head = (ra.B >= 64) ? (ra.B / 64 < 16 ? ra.B / 64 : 16) : 0;
+        if (head > ra.B) head = ra.B;
+        if (head > 0) {
+            static bool carve = false;
+            if (!carve) {
+                cudaFuncSetAttribute(k_integrate_mixed, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+                carve = true;
+            }
+            const int nq = head < nsm ? head : nsm;
+            const long long need = nq + ((long long)(ra.B - head) * 64 + 127) / 128;
+            const int grid = (int)(need < nsm ? need : nsm);
+            k_integrate_mixed<<<grid > nq ? grid : nq, 128, 0, s>>>(a, nq, head);
+            return cudaGetLastError();
+        }
+    }
     switch (G) {
         case 1: return launch_g<1>(a, bs, ra.opt.grid, s);
         case 2: return launch_g<2>(a, bs, ra.opt.grid, s);
@@ -614,7 +685,8 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
         case 8: return launch_g<8>(a, bs, ra.opt.grid, s);
         case 16: return launch_g<16>(a, bs, ra.opt.grid, s);
         case 32: return launch_g<32>(a, bs, ra.opt.grid, s);
-        default: return launch_g<64>(a, bs % 64 == 0 ? bs : 128, ra.opt.grid, s);
+        case 64: return launch_g<64>(a, bs % 64 == 0 ? bs : 128, ra.opt.grid, s);
+        default: return launch_g<128>(a, bs % 128 == 0 ? bs : 128, ra.opt.grid, s);
     }
 }
 

@@ -359,6 +359,7 @@ EOB_HD const double *tprod_row(int l)
 struct FluxLane {
     double v, lv, v12, Se, Sodd;
     double vp[8];  // vphi^(2 e), e = 2..9
+    double S2e, S2o;  // Se^2, Sodd^2
 };
 
 // the shared pieces from v and v_phi = omega / omega_c^(2/3), with log v
@@ -383,6 +384,8 @@ EOB_HD FluxLane flux_lane_make_rv(const FluxTable &t, double pphi, double omega,
     f.vp[7] = p4 * p4 * p1;
     f.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
     f.Sodd = v * pphi;
+    f.S2e = f.Se * f.Se;
+    f.S2o = f.Sodd * f.Sodd;
     return f;
 }
 
@@ -425,10 +428,13 @@ EOB_HD int lm_packed(int i)
 #endif
 }
 
-// m^2 |h_lm|^2 / omega^2 of multipole i (rho_lm series of at most KMAX
-// terms) from the shared pieces and the m factors T, k4 of its m
+// m^2 |h_lm|^2 / omega^2 of multipole i as a product of two factors that
+// separate warps can evaluate: flux_mode_a (rho_lm^l with the f_lm term, S^2
+// and v_phi^(2 (l + eps)): the series in v) and flux_mode_b (m^2 |h^N_lm|^2 /
+// (l!)^2 times (m x)/(1 - e^{-m x}) prod_{j<=l} (4 k^2 + j^2): the m factors).
+// KMAX bounds the rho_lm series of the modes evaluated together.
 template <int KMAX>
-EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
+EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
 {
     const int lm = lm_packed(i);
     const int l = lm >> 4, m = lm & 15;
@@ -453,18 +459,30 @@ EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, doubl
     if (l == 8) rpl = r4 * r4;
     const double aux = f.v * fma(t.f3[i], f.v * f.v, t.f1[i]);
     rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
-    const double S = eps ? f.Sodd : f.Se;
+    const double S2 = eps ? f.S2o : f.S2e;
     // vphi^(2 (l + eps)) selected from the precomputed powers
     const int e = l + eps - 2;
     double vpw = f.vp[0];
 #pragma unroll
     for (int q = 1; q < 8; ++q) vpw = (e == q) ? f.vp[q] : vpw;
+    return S2 * (rpl * rpl) * vpw;
+}
+
+EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
+{
+    const int l = lm_packed(i) >> 4;
     // prod_{j<=l} (4 k^2 + j^2)
     const double *c = tprod_row(l);
     double P = c[kLMax];
 #pragma unroll
     for (int q = kLMax - 1; q >= 0; --q) P = fma(P, k4, c[q]);
-    return t.gmul[i] * T * P * (S * S) * (rpl * rpl) * vpw;
+    return t.gmul[i] * T * P;
+}
+
+template <int KMAX>
+EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
+{
+    return flux_mode_b(t, i, T, k4) * flux_mode_a<KMAX>(t, i, f);
 }
 
 // Sequential use of the lane-group pieces (host tests)

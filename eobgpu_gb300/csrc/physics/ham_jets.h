@@ -125,33 +125,62 @@ struct HamPart {
     double H, Hreal, dHdr, dHdpr, dHdL;
 };
 
-// The combination in four pieces, so that two warps carrying one binary can
-// evaluate them side by side (comb_a with comb_b, then comb_even with
-// comb_odd); ham_combine() runs them in sequence.
+// The combination in pieces, so that the warps carrying one binary can
+// evaluate them side by side: a warp pair runs comb_a with comb_b, then
+// comb_even with comb_odd; four warps split them finer (comb_A, comb_C,
+// comb_W, comb_N, then comb_even_parts with comb_odd_parts).  ham_combine()
+// runs them in sequence.  Every path composes the same pieces.
 
-// A(u) = S Fa As / Dc and the centrifugal coefficient c(u) = u^2 (1 + a^2 Bnpa)
+// A(u) = S Fa As / Dc and its u-derivative, given 1 / Dc
+struct PartA {
+    double Av, Ad;
+};
+
+EOB_HD PartA comb_A(const Jet *jt, double idc)
+{
+    const Jet ak0 = jt[J_AK0], aka = jt[J_AKA], fa = jt[J_FA], as = jt[J_AS], dc = jt[J_DC];
+    const double Sv = ak0.v + aka.v, Sd = ak0.d + aka.d;
+    const double sf = Sv * fa.v;
+    const double na = sf * as.v;
+    const double dna = fma(Sd * fa.v + Sv * fa.d, as.v, sf * as.d);
+    PartA o;
+    o.Av = na * idc;
+    o.Ad = fma(-o.Av, dc.d, dna) * idc;
+    return o;
+}
+
+// the centrifugal coefficient c(u) = u^2 (1 + a^2 Bnpa), Bnpa = -(u^2 + 2 u^3) / Dc
+struct PartC {
+    double cuv, cud;
+};
+
+EOB_HD PartC comb_C(const HamJets &J, const Jet *jt, double u, double idc)
+{
+    const Jet dc = jt[J_DC], bnn = jt[J_BNN];
+    const double u2 = u * u;
+    const double bnpa = bnn.v * idc;
+    const double dbnpa = fma(-bnpa, dc.d, bnn.d) * idc;
+    const double cf = fma(J.apsq, bnpa, 1.0);
+    PartC o;
+    o.cuv = u2 * cf;
+    o.cud = fma(2.0 * u, cf, u2 * J.apsq * dbnpa);
+    return o;
+}
+
 struct CombA {
     double idc, Av, Ad, cuv, cud;
 };
 
 EOB_HD CombA comb_a(const HamJets &J, const Jet *jt, double u)
 {
-    const Jet ak0 = jt[J_AK0], aka = jt[J_AKA], fa = jt[J_FA], as = jt[J_AS], dc = jt[J_DC], bnn = jt[J_BNN];
-    const double u2 = u * u;
     CombA o;
-    o.idc = 1.0 / dc.v;
-    const double idc = o.idc;
-    const double Sv = ak0.v + aka.v, Sd = ak0.d + aka.d;
-    const double sf = Sv * fa.v;
-    const double na = sf * as.v;
-    const double dna = fma(Sd * fa.v + Sv * fa.d, as.v, sf * as.d);
-    o.Av = na * idc;
-    o.Ad = fma(-o.Av, dc.d, dna) * idc;
-    const double bnpa = bnn.v * idc;
-    const double dbnpa = fma(-bnpa, dc.d, bnn.d) * idc;
-    const double cf = fma(J.apsq, bnpa, 1.0);
-    o.cuv = u2 * cf;
-    o.cud = fma(2.0 * u, cf, u2 * J.apsq * dbnpa);
+    o.idc = 1.0 / jt[J_DC].v;
+    const PartA pa = comb_A(jt, o.idc);
+    const PartC pc = comb_C(J, jt, u, o.idc);
+    o.Av = pa.Av;
+    o.Ad = pa.Ad;
+    o.cuv = pc.cuv;
+    o.cud = pc.cud;
     return o;
 }
 
@@ -173,20 +202,35 @@ EOB_HD CombB comb_b(const Jet *jt, double p2)
     return o;
 }
 
+// the part of W = 1 + p_r^2 (1 + B_np) + L^2 c + p_r^4 q that does not need c:
+// W - L^2 c, its u-derivative minus L^2 c', and dW/dp_r
+struct PartW {
+    double W, Wu, Wp;
+};
+
+EOB_HD PartW comb_W(const Jet *jt, const CombB &b, double pr)
+{
+    const Jet q4 = jt[J_Q4], q6 = jt[J_Q6], q8 = jt[J_Q8];
+    const double p2 = pr * pr;
+    PartW o;
+    o.W = fma(p2 * p2, b.qa, fma(p2, 1.0 + b.bnpv, 1.0));
+    o.Wu = fma(p2 * p2, b.qad, p2 * b.bnpd);
+    o.Wp = 2.0 * pr * ((1.0 + b.bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
+    return o;
+}
+
 // a piece of H_eff with its derivatives in u, p_r and L
 struct HeffPart {
     double v, du, dp, dL;
 };
 
-// even part sqrt(A W) (W = 1 + p_r^2 (1 + B_np) + L^2 c + p_r^4 q)
-EOB_HD HeffPart comb_even(const Jet *jt, const CombA &a, const CombB &b, double pr, double L)
+// even part sqrt(A W)
+EOB_HD HeffPart comb_even_parts(const PartA &a, const PartC &c, const PartW &w, double L)
 {
-    const Jet q4 = jt[J_Q4], q6 = jt[J_Q6], q8 = jt[J_Q8];
-    const double p2 = pr * pr, L2 = L * L;
-    const double W = 1.0 + p2 * (1.0 + b.bnpv) + L2 * a.cuv + p2 * p2 * b.qa;
-    const double Wu = p2 * b.bnpd + L2 * a.cud + p2 * p2 * b.qad;
-    const double Wp = 2.0 * pr * ((1.0 + b.bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
-    const double WL = 2.0 * L * a.cuv;
+    const double L2 = L * L;
+    const double W = fma(L2, c.cuv, w.W);
+    const double Wu = fma(L2, c.cud, w.Wu);
+    const double WL = 2.0 * L * c.cuv;
     // sqrt and the reciprocal from one reciprocal square root
     const double AW = a.Av * W;
     const double rAW = eob_rsqrt(AW);
@@ -194,28 +238,49 @@ EOB_HD HeffPart comb_even(const Jet *jt, const CombA &a, const CombB &b, double 
     HeffPart o;
     o.v = AW * rAW;
     o.du = fma(a.Ad, W, a.Av * Wu) * ih2;
-    o.dp = a.Av * Wp * ih2;
+    o.dp = a.Av * w.Wp * ih2;
     o.dL = a.Av * WL * ih2;
     return o;
 }
 
-// odd part L u^3 N(u, p_r^2) / Dc
-EOB_HD HeffPart comb_odd(const HamJets &J, const Jet *jt, double u, double idc, double pr, double L)
+EOB_HD HeffPart comb_even(const Jet *jt, const CombA &a, const CombB &b, double pr, double L)
 {
-    const Jet dc = jt[J_DC], n0 = jt[J_N0], n1 = jt[J_N1], n2 = jt[J_N2], n3 = jt[J_N3];
-    const double u2 = u * u, u3 = u2 * u;
-    const double p2 = pr * pr;
+    return comb_even_parts({a.Av, a.Ad}, {a.cuv, a.cud}, comb_W(jt, b, pr), L);
+}
+
+// N(u, p_r^2) = sum_j p_r^(2j) N_j(u) with its u- and p_r^2-derivatives
+struct PartN {
+    double Nv, Nu, Np;
+};
+
+EOB_HD PartN comb_N(const HamJets &J, const Jet *jt, double p2)
+{
+    const Jet n0 = jt[J_N0], n1 = jt[J_N1], n2 = jt[J_N2], n3 = jt[J_N3];
     const double n4 = J.n4;
-    const double Nv = n0.v + p2 * (n1.v + p2 * (n2.v + p2 * (n3.v + p2 * n4)));
-    const double Nu = n0.d + p2 * (n1.d + p2 * (n2.d + p2 * n3.d));
-    const double Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * 4.0 * n4));
+    PartN o;
+    o.Nv = n0.v + p2 * (n1.v + p2 * (n2.v + p2 * (n3.v + p2 * n4)));
+    o.Nu = n0.d + p2 * (n1.d + p2 * (n2.d + p2 * n3.d));
+    o.Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * 4.0 * n4));
+    return o;
+}
+
+// odd part L u^3 N / Dc
+EOB_HD HeffPart comb_odd_parts(const Jet *jt, double u, double idc, const PartN &n, double pr, double L)
+{
+    const Jet dc = jt[J_DC];
+    const double u2 = u * u, u3 = u2 * u;
     const double u3i = u3 * idc;
     HeffPart o;
-    o.v = L * u3i * Nv;
-    o.du = L * idc * (3.0 * u2 * Nv + u3 * Nu - u3 * Nv * idc * dc.d);
-    o.dp = L * u3i * Np * 2.0 * pr;
-    o.dL = u3i * Nv;
+    o.v = L * u3i * n.Nv;
+    o.du = L * idc * (3.0 * u2 * n.Nv + u3 * n.Nu - u3 * n.Nv * idc * dc.d);
+    o.dp = L * u3i * n.Np * 2.0 * pr;
+    o.dL = u3i * n.Nv;
     return o;
+}
+
+EOB_HD HeffPart comb_odd(const HamJets &J, const Jet *jt, double u, double idc, double pr, double L)
+{
+    return comb_odd_parts(jt, u, idc, comb_N(J, jt, pr * pr), pr, L);
 }
 
 // H = M sqrt(1 + 2 nu (H_eff - 1)) / nu and its derivatives

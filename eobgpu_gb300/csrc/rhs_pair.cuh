@@ -113,17 +113,20 @@ __device__ __forceinline__ void pair_sync_spin(PairSync &ps)
     if (!__all_sync(0xffffffffu, done)) ps.ok = false;
 }
 
-// Set-up by the block's first thread, before any pair barrier is used.
-__device__ __forceinline__ void pair_init(unsigned long long *bars, int npairs)
+// Set-up by the block's first thread, before any group barrier is used:
+// ngroups barriers of `arrivals` threads each (64 for a pair, 128 for four warps).
+__device__ __forceinline__ void group_init(unsigned long long *bars, int ngroups, int arrivals)
 {
     if (threadIdx.x == 0) {
-        for (int p = 0; p < npairs; ++p) {
+        for (int p = 0; p < ngroups; ++p) {
             const unsigned a = (unsigned)__cvta_generic_to_shared(&bars[p]);
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(64) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(arrivals) : "memory");
         }
     }
     __syncthreads();
 }
+
+__device__ __forceinline__ void pair_init(unsigned long long *bars, int npairs) { group_init(bars, npairs, 64); }
 
 // multipoles at sorted positions [FIRST, FIRST + 32) of one warp, m factors
 // from shared memory
@@ -271,6 +274,8 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         f.v12 = x.fl[2];
         f.Se = x.fl[3];
         f.Sodd = x.fl[4];
+        f.S2e = f.Se * f.Se;
+        f.S2o = f.Sodd * f.Sodd;
 #pragma unroll
         for (int q = 0; q < 8; ++q) f.vp[q] = x.fl[5 + q];
         part = flux_warp_modes<32>(t, f, x, lane);

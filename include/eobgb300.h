@@ -35,8 +35,8 @@ extern "C" {
 #define EOB_ST_TRIES 8         /* step-attempt limit reached (no progress) */
 #define EOB_ST_SHORT 16        /* too few rows for the step-back restart or the spline */
 #define EOB_ST_STOP_REJECT 32  /* first step of a pass rejected (reference stops there) */
-#define EOB_ST_SYNC 64         /* the two warps of a warp pair (lanes_per_binary 64) lost step: a barrier wait
-                                  ran out of time and the binary was ended early */
+#define EOB_ST_SYNC 64         /* the warps of a multi-warp group (lanes_per_binary 64 or 128) lost step: a
+                                  barrier wait ran out of time and the binary was ended early */
 
 typedef struct eob_options {
     double rtol, atol;      /* DOPR853 tolerances; reference: 1e-12, 1e-12 (src/DOPR853.cu:7-8) */
@@ -50,9 +50,12 @@ typedef struct eob_options {
     int block;              /* integrator threads per block (0 = default) */
     int grid;               /* integrator blocks (0 = one wave of resident blocks) */
     long long max_tries;    /* step attempts per pass before giving up (0 = 2 * max_steps + 100) */
-    int lanes_per_binary;   /* integrator lanes per binary: 1, 2, 4, 8, 16, 32, or 64 (two warps on two SM
-                               sub-partitions; 0 = chosen from the batch size) */
+    int lanes_per_binary;   /* integrator lanes per binary: 1, 2, 4, 8, 16, 32, 64 (two warps on two SM
+                               sub-partitions) or 128 (four warps, one per sub-partition of an SM);
+                               0 = chosen from the batch size */
     int spline_tile;        /* spline build: series (one warp each) per block, 1..8 (0 = default 4) */
+    int head_quads;         /* with warp pairs: the head_quads longest binaries (first in `order`) on four
+                               warps each, concurrently with the pairs (-1 = chosen from the batch, 0 = none) */
 } eob_options;
 
 void eob_options_default(eob_options *o);

@@ -122,7 +122,7 @@ def test_config1_lnl_vs_oracle(cfg1_run, oracle):
         assert abs(lnl[b] / r["lnl"] - 1) < 1e-9, (b, lnl[b], r["lnl"])
 
 
-@pytest.mark.parametrize("G", [1, 2, 4, 8, 16, 32, 64])
+@pytest.mark.parametrize("G", [1, 2, 4, 8, 16, 32, 64, 128])
 def test_config1_lanes_per_binary(torch_cuda, golden, G):
     """Every lanes-per-binary variant of the integrator gives the reference's lnL."""
     torch = torch_cuda
