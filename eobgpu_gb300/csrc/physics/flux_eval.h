@@ -433,8 +433,9 @@ EOB_HD int lm_packed(int i)
 // and v_phi^(2 (l + eps)): the series in v) and flux_mode_b (m^2 |h^N_lm|^2 /
 // (l!)^2 times (m x)/(1 - e^{-m x}) prod_{j<=l} (4 k^2 + j^2): the m factors).
 // KMAX bounds the rho_lm series of the modes evaluated together.
+// the series part without the v_phi power: S^2 (rho_lm^l + f_lm)^2
 template <int KMAX>
-EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
+EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
 {
     const int lm = lm_packed(i);
     const int l = lm >> 4, m = lm & 15;
@@ -460,12 +461,38 @@ EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
     const double aux = f.v * fma(t.f3[i], f.v * f.v, t.f1[i]);
     rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
     const double S2 = eps ? f.S2o : f.S2e;
-    // vphi^(2 (l + eps)) selected from the precomputed powers
-    const int e = l + eps - 2;
+    return S2 * (rpl * rpl);
+}
+
+// vphi^(2 (l + eps)) of multipole i selected from the precomputed powers
+EOB_HD double flux_mode_vp(int i, const FluxLane &f)
+{
+    const int lm = lm_packed(i);
+    const int l = lm >> 4, m = lm & 15;
+    const int e = l + ((l + m) & 1) - 2;
     double vpw = f.vp[0];
 #pragma unroll
     for (int q = 1; q < 8; ++q) vpw = (e == q) ? f.vp[q] : vpw;
-    return S2 * (rpl * rpl) * vpw;
+    return vpw;
+}
+
+template <int KMAX>
+EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
+{
+    return flux_mode_s<KMAX>(t, i, f) * flux_mode_vp(i, f);
+}
+
+// vphi^(2 (l + eps)) of multipole i from vphi^2 by squaring (l + eps = 2..9)
+EOB_HD double flux_mode_vp_sq(int i, double vphi2)
+{
+    const int lm = lm_packed(i);
+    const int e = (lm >> 4) + (((lm >> 4) + (lm & 15)) & 1);
+    const double p2 = vphi2 * vphi2, p4 = p2 * p2;
+    double r = (e & 1) ? vphi2 : 1.0;
+    if (e & 2) r *= p2;
+    if (e & 4) r *= p4;
+    if (e & 8) r *= p4 * p4;
+    return r;
 }
 
 EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)

@@ -8,8 +8,9 @@
 //   combination a   1/Dc, A(u)          1/Dc, c(u)          B_np, q, W - L^2 c  N(u, p_r^2)
 //   combination b   even part sqrt(AW)  odd part            --                  y_2/y_3, 1/(8 pi nu)
 //   H, flux set-up  H and gradient,     m factors from      omega, v = omega    omega, log v,
-//                   v_phi powers        H_real omega = M^2 D r_omega^2, v^12, S_o H_real, S_even
-//   multipoles      series part 0..31   m-factor part 0..31 series part 32..34  m-factor part 32..34
+//                   v_phi^2             H_real omega = M^2 D r_omega^2, v^12, S_o H_real, S_even
+//   multipoles      series part 0..31   m-factor and v_phi  series part 32..34  m-factor and v_phi
+//                                       part 0..31                              part 32..34
 //   (then each multipole's two parts multiplied and summed)
 //
 // Values cross through shared memory at six barriers per right-hand side
@@ -31,7 +32,7 @@ struct QuadXchg {
     double ev[4][32];      // warp 0: even part of H_eff and its derivatives
     double od[4][32];      // warp 1: odd part
     double ham[3];         // warp 0: dH/dr, dH/dp_r, dH/dL at the state
-    double fl[16];         // v, log v, v^12, S_e^2, S_o^2, v_phi^(2e) e = 2..9
+    double fl[16];         // v, log v, v^12, S_e^2, S_o^2, v_phi^2
     double T[8], k4[8];    // warp 1: m factors, m = 1..8
     double b[40];          // m-factor parts of the multipoles (sorted positions)
     double part[2];        // flux partial sums (warps 0 and 2)
@@ -154,21 +155,11 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
             x.ham[1] = hp.dHdpr;
             x.ham[2] = hp.dHdL;
         }
-        // v_phi = omega omega_c^(-2/3) and its even powers
+        // v_phi^2 = (omega omega_c^(-2/3))^2 (its powers are taken by the
+        // m-factor warps, which wait longer)
         const double rc = eob_rcbrt(omega_c);
         const double vphi = omega * (rc * rc);
-        const double p1 = vphi * vphi;
-        const double p2 = p1 * p1, p3 = p2 * p1, p4 = p2 * p2;
-        if (lane == 0) {
-            x.fl[5] = p2;
-            x.fl[6] = p3;
-            x.fl[7] = p4;
-            x.fl[8] = p4 * p1;
-            x.fl[9] = p3 * p3;
-            x.fl[10] = p3 * p4;
-            x.fl[11] = p4 * p4;
-            x.fl[12] = p4 * p4 * p1;
-        }
+        if (lane == 0) x.fl[5] = vphi * vphi;
     } else if (q == 1) {
         // H_real omega = M^2 D (H_real = M s, omega = M D / s)
         const double hw = (J.M * J.M) * D;
@@ -217,20 +208,18 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     f.S2o = x.fl[4];
     f.Se = 0.0;
     f.Sodd = 0.0;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) f.vp[s] = x.fl[5 + s];
     double a_part = 0.0;
     if (q == 0) {
-        a_part = flux_mode_a<kFluxDegSorted[0]>(t, kFluxOrder[lane], f);
+        a_part = flux_mode_s<kFluxDegSorted[0]>(t, kFluxOrder[lane], f);
     } else if (q == 2) {
         const int pos = 32 + lane;
-        a_part = flux_mode_a<kFluxDegSorted[32]>(t, kFluxOrder[pos < kNumLM ? pos : kNumLM - 1], f);
+        a_part = flux_mode_s<kFluxDegSorted[32]>(t, kFluxOrder[pos < kNumLM ? pos : kNumLM - 1], f);
     } else {
         const int pos = (q == 1) ? lane : 32 + lane;
         if (pos < kNumLM) {
             const int i = kFluxOrder[pos];
             const int m = lm_packed(i) & 15;
-            x.b[pos] = flux_mode_b(t, i, x.T[m - 1], x.k4[m - 1]);
+            x.b[pos] = flux_mode_b(t, i, x.T[m - 1], x.k4[m - 1]) * flux_mode_vp_sq(i, x.fl[5]);
         }
     }
     pair_sync(ps);  // 5: m-factor parts

@@ -95,6 +95,26 @@ static double flux_pair_host(const eob::FluxTable &t, double pphi, double omega,
     return (part[0] + part[1]) * omega * omega / (8.0 * eob::kPi);
 }
 
+// flux as four warps sum it: series parts S^2 (rho^l + f)^2 times m-factor
+// parts with v_phi^(2 (l + eps)) from v_phi^2 by squaring
+static double flux_quad_host(const eob::FluxTable &t, double pphi, double omega, double Hreal, double omega_c)
+{
+    const double r0 = 1.0 / cbrt(omega), r1 = 1.0 / cbrt(omega_c);
+    const double vphi = omega * (r1 * r1);
+    const eob::FluxLane f = eob::flux_lane_make_rv(t, pphi, omega, Hreal, omega * (r0 * r0), vphi,
+                                                   eob::eob_log(omega) * (1.0 / 3.0));
+    double T[8], k4[8];
+    for (int m = 1; m <= 8; ++m)
+        eob::flux_m_factors(m, 4.0 * eob::kPi * Hreal * omega, Hreal * omega, &T[m - 1], &k4[m - 1]);
+    double sum = 0.0;
+    for (int i = 0; i < 35; ++i) {
+        const int m = eob::lm_packed(i) & 15;
+        sum += (eob::flux_mode_b(t, i, T[m - 1], k4[m - 1]) * eob::flux_mode_vp_sq(i, vphi * vphi)) *
+               eob::flux_mode_s<10>(t, i, f);
+    }
+    return sum * omega * omega / (8.0 * eob::kPi);
+}
+
 void phys_flux_pair(const double *st, const double *add, int n, double *out)
 {
     for (int i = 0; i < n; ++i) {
@@ -114,6 +134,7 @@ void phys_flux_pair(const double *st, const double *add, int n, double *out)
         eob::ham_eval(h, st[i], st[2 * n + i], st[3 * n + i], &e);
         out[2 * i] = eob::flux_eval_lanes(t, st[3 * n + i], e.dHdL, e.Hreal, e.omega_c);
         out[2 * i + 1] = flux_pair_host(t, st[3 * n + i], e.dHdL, e.Hreal, e.omega_c);
+        out[2 * n + i] = flux_quad_host(t, st[3 * n + i], e.dHdL, e.Hreal, e.omega_c);
     }
 }
 

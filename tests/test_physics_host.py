@@ -90,17 +90,21 @@ def test_ham_pair_pieces_match_jets(phys, golden):
 
 
 def test_flux_pair_matches_lanes(phys, golden):
-    """Flux summed as a warp pair does (multipoles 0..31 and 32..34 apart)."""
+    """Flux summed as a warp pair does (multipoles 0..31 and 32..34 apart) and
+    as four warps do (series parts times m-factor parts with the v_phi powers
+    by squaring)."""
     g = golden["ham_rhs"]
     st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
     n = st.shape[1]
-    out = np.zeros(2 * n)
-    phys.phys_flux_pair(dp(st), dp(add), ctypes.c_int(n), dp(out))
-    out = out.reshape(n, 2)
+    buf = np.zeros(3 * n)
+    phys.phys_flux_pair(dp(st), dp(add), ctypes.c_int(n), dp(buf))
+    out = buf[:2 * n].reshape(n, 2)
+    quad = buf[2 * n:]
     ok = np.isfinite(out[:, 0])
     assert ok.sum() > 0.9 * n
     np.testing.assert_array_equal(np.isfinite(out[:, 1]), ok)
     assert np.max(np.abs(out[ok, 1] / out[ok, 0] - 1)) < 1e-13
+    assert np.max(np.abs(quad[ok] / out[ok, 0] - 1)) < 1e-13
 
 
 def test_eob_log_accuracy(phys):
