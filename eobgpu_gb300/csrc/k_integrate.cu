@@ -86,8 +86,8 @@ constexpr double er1 = 0.1312004499419488073250102996e-01, er6 = -0.122515644637
 constexpr double safe = 0.9, minscale = 1.0 / 3.0, maxscale = 6.0;
 }  // namespace dp
 
-// err^(-1/8) without pow(): three square roots and a division
-__device__ __forceinline__ double inv_eighth_root(double x) { return 1.0 / sqrt(sqrt(sqrt(x))); }
+// err^(-1/8) without pow(): a reciprocal square root and two square roots
+__device__ __forceinline__ double inv_eighth_root(double x) { return sqrt(sqrt(rsqrt(x))); }
 
 __device__ __forceinline__ double pow4(double x)
 {
@@ -131,6 +131,45 @@ struct IntArgs {
     long long max_tries;
 };
 
+// Stage sums with the slope slots fixed at compile time, for groups whose
+// lanes all work on the same stage (32 lanes or more per binary): the slopes
+// then stay in registers instead of local memory.
+__device__ __forceinline__ double stage_sum_fixed(int stage, const double (&kr)[11][1])
+{
+    switch (stage) {
+        case 2: return (0.0 + dp::kStage[2][0].a * kr[1][0]);
+        case 3: return ((0.0 + dp::kStage[3][0].a * kr[1][0]) + dp::kStage[3][1].a * kr[2][0]);
+        case 4: return ((0.0 + dp::kStage[4][0].a * kr[1][0]) + dp::kStage[4][1].a * kr[3][0]);
+        case 5: return (((0.0 + dp::kStage[5][0].a * kr[1][0]) + dp::kStage[5][1].a * kr[3][0]) + dp::kStage[5][2].a * kr[4][0]);
+        case 6: return (((0.0 + dp::kStage[6][0].a * kr[1][0]) + dp::kStage[6][1].a * kr[4][0]) + dp::kStage[6][2].a * kr[5][0]);
+        case 7: return ((((0.0 + dp::kStage[7][0].a * kr[1][0]) + dp::kStage[7][1].a * kr[4][0]) + dp::kStage[7][2].a * kr[5][0]) + dp::kStage[7][3].a * kr[6][0]);
+        case 8: return (((((0.0 + dp::kStage[8][0].a * kr[1][0]) + dp::kStage[8][1].a * kr[4][0]) + dp::kStage[8][2].a * kr[5][0]) + dp::kStage[8][3].a * kr[6][0]) + dp::kStage[8][4].a * kr[7][0]);
+        case 9: return ((((((0.0 + dp::kStage[9][0].a * kr[1][0]) + dp::kStage[9][1].a * kr[4][0]) + dp::kStage[9][2].a * kr[5][0]) + dp::kStage[9][3].a * kr[6][0]) + dp::kStage[9][4].a * kr[7][0]) + dp::kStage[9][5].a * kr[8][0]);
+        case 10: return (((((((0.0 + dp::kStage[10][0].a * kr[1][0]) + dp::kStage[10][1].a * kr[4][0]) + dp::kStage[10][2].a * kr[5][0]) + dp::kStage[10][3].a * kr[6][0]) + dp::kStage[10][4].a * kr[7][0]) + dp::kStage[10][5].a * kr[8][0]) + dp::kStage[10][6].a * kr[9][0]);
+        case 11: return ((((((((0.0 + dp::kStage[11][0].a * kr[1][0]) + dp::kStage[11][1].a * kr[4][0]) + dp::kStage[11][2].a * kr[5][0]) + dp::kStage[11][3].a * kr[6][0]) + dp::kStage[11][4].a * kr[7][0]) + dp::kStage[11][5].a * kr[8][0]) + dp::kStage[11][6].a * kr[9][0]) + dp::kStage[11][7].a * kr[10][0]);
+        case 12: return (((((((((0.0 + dp::kStage[12][0].a * kr[1][0]) + dp::kStage[12][1].a * kr[4][0]) + dp::kStage[12][2].a * kr[5][0]) + dp::kStage[12][3].a * kr[6][0]) + dp::kStage[12][4].a * kr[7][0]) + dp::kStage[12][5].a * kr[8][0]) + dp::kStage[12][6].a * kr[9][0]) + dp::kStage[12][7].a * kr[10][0]) + dp::kStage[12][8].a * kr[2][0]);
+        default: return 0.0;
+    }
+}
+
+__device__ __forceinline__ void store_slope_fixed(int stage, double (&kr)[11][1], double km)
+{
+    switch (stage) {
+        case 2: kr[2][0] = km; break;
+        case 3: kr[3][0] = km; break;
+        case 4: kr[4][0] = km; break;
+        case 5: kr[5][0] = km; break;
+        case 6: kr[6][0] = km; break;
+        case 7: kr[7][0] = km; break;
+        case 8: kr[8][0] = km; break;
+        case 9: kr[9][0] = km; break;
+        case 10: kr[10][0] = km; break;
+        case 11: kr[2][0] = km; break;
+        case 12: kr[3][0] = km; break;
+        default: break;
+    }
+}
+
 // component q of a 4-vector held in registers (selects, no local memory)
 __device__ __forceinline__ double pick4(const double v[4], int q)
 {
@@ -162,6 +201,8 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     constexpr int GW = kPair ? 32 : G;  // lanes of the group inside one warp
     constexpr bool kDist = (G >= 4);
     constexpr int NC = kDist ? 1 : 4;  // state components held by one lane
+    // every lane of a warp on the same stage: slopes in registers (stage_sum_fixed)
+    constexpr bool kReg = (GW == 32);
     const int lane = threadIdx.x & 31;
     const int sub = lane & (GW - 1);
     const int role = kPair ? (int)((threadIdx.x >> 5) % NW) : 0;
@@ -250,11 +291,15 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
         // ------------------------------------------------ RHS argument
         int out_slot = 1;
         if (phase == kStage) {
-            const int nt = dp::kNTerms[stage];
-            for (int c = 0; c < NC; ++c) {
-                double ak = 0.0;
-                for (int t = 0; t < nt; ++t) ak += dp::kStage[stage][t].a * k[dp::kStage[stage][t].slot][c];
-                argl[c] = y[c] + h * ak;
+            if constexpr (kReg) {
+                argl[0] = y[0] + h * stage_sum_fixed(stage, k);
+            } else {
+                const int nt = dp::kNTerms[stage];
+                for (int c = 0; c < NC; ++c) {
+                    double ak = 0.0;
+                    for (int t = 0; t < nt; ++t) ak += dp::kStage[stage][t].a * k[dp::kStage[stage][t].slot][c];
+                    argl[c] = y[c] + h * ak;
+                }
             }
             out_slot = dp::kOutSlot[stage];
         } else if (phase == kStopTest || phase == kStartPass) {
@@ -316,8 +361,9 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
         if (phase == kStage) {
             double wb, we, wh;
             stage_weights(stage, &wb, &we, &wh);
+            if constexpr (kReg) store_slope_fixed(stage, k, km[0]);
             for (int c = 0; c < NC; ++c) {
-                k[out_slot][c] = km[c];
+                if constexpr (!kReg) k[out_slot][c] = km[c];
                 acc_b[c] = fma(wb, km[c], acc_b[c]);
                 acc_e[c] = fma(we, km[c], acc_e[c]);
                 acc_h[c] = fma(wh, km[c], acc_h[c]);
@@ -350,7 +396,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             }
             double denom = e1 + 0.01 * e2;
             denom = (denom < 0.0) ? 1.0 : denom;
-            const double err = fabs(h) * e1 * sqrt(1.0 / (4.0 * denom));
+            const double err = fabs(h) * e1 * (0.5 * rsqrt(denom));  // |h| e1 sqrt(1 / (4 denom))
             const double hOld = h;
             // controller (src/DOPR853.cu:674-762), beta = 0
             bool ok;
