@@ -52,7 +52,7 @@ def _census_flops():
 
 F_RHS = _census_flops()
 
-TRAFFIC = os.path.join(ROOT, "profiles", "k_integrate_pair_traffic_config2.md")
+TRAFFIC = os.path.join(ROOT, "profiles", "k_integrate_traffic_config2.md")
 
 
 def _traffic_bytes():
@@ -687,7 +687,7 @@ def main():
                 "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                 "traffic": _traffic_bytes() if default_workload else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                  "profiles/k_integrate_pair_traffic_config2.md" if default_workload else None,
+                                  "profiles/k_integrate_traffic_config2.md" if default_workload else None,
                 "peak_source": "measured live: FP64 DFMA probe (eob_fp64_probe), burst",
                 "work": f"{F_RHS:.0f} FP64 FLOP per RHS x {cnt['rhs_binaries']} RHS evaluations",
                 "lane_occupancy": cnt["rhs_binaries"] / max(1, cnt["rhs_all_lanes"])}

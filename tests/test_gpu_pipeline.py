@@ -141,6 +141,35 @@ def test_config1_lanes_per_binary(torch_cuda, golden, G):
     np.testing.assert_array_equal(nsteps, c["nsteps"])
 
 
+def test_config1_mixed_head(torch_cuda, golden):
+    """Warp pairs with the longest binaries on four warps in the same launch
+    (eob_options.head_quads): the reference's lnL and row counts, and the same
+    bits as each group size run alone for its binaries."""
+    torch = torch_cuda
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood, longest_first
+    c = golden["config1"]
+    P = torch.tensor(c["params"], device="cuda")
+    D = torch.tensor(c["data"], device="cuda")
+    order = longest_first(P)
+    runs = {}
+    for name, G, head in (("mixed", 64, 3), ("pairs", 64, 0), ("quads", 128, 0)):
+        opt = _lib.default_options()
+        opt.lanes_per_binary = G
+        opt.head_quads = head
+        wl = WaveformLikelihood(max_batch=8, max_steps=4096, modes=[(2, 2)], max_samples=int(c["N"]), options=opt)
+        lnl, st = wl.run(P, D, float(c["dt"]), float(c["amp"]), order=order)
+        assert np.all(st.cpu().numpy() == 0), name
+        runs[name] = (lnl.cpu().numpy(), wl.trajectories()[0])
+    lnl, nsteps = runs["mixed"]
+    assert np.all(np.abs(lnl / c["lnl"] - 1) < 1e-9), lnl / c["lnl"] - 1
+    np.testing.assert_array_equal(nsteps, c["nsteps"])
+    head = order.cpu().numpy()[:3]
+    rest = order.cpu().numpy()[3:]
+    np.testing.assert_array_equal(lnl[head], runs["quads"][0][head])
+    np.testing.assert_array_equal(lnl[rest], runs["pairs"][0][rest])
+
+
 def test_config1_rtol_1e10_vs_oracle(torch_cuda, golden, oracle):
     """Configuration 1 as its benchmark states it, DOPR853 at rtol = atol =
     1e-10 (the reference hard-codes 1e-12), against the oracle at the same
