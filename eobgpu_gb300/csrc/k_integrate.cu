@@ -39,38 +39,42 @@ struct Term {
     signed char slot;
     double a;
 };
-__constant__ Term kStage[13][9] = {
-    {}, {},
-    {{1, 5.26001519587677318785587544488e-2}},
-    {{1, 1.97250569845378994544595329183e-2}, {2, 5.91751709536136983633785987549e-2}},
-    {{1, 2.95875854768068491816892993775e-2}, {3, 8.87627564304205475450678981324e-2}},
-    {{1, 2.41365134159266685502369798665e-1}, {3, -8.84549479328286085344864962717e-1},
-     {4, 9.24834003261792003115737966543e-1}},
-    {{1, 3.7037037037037037037037037037e-2}, {4, 1.70828608729473871279604482173e-1},
-     {5, 1.25467687566822425016691814123e-1}},
-    {{1, 3.7109375e-2}, {4, 1.70252211019544039314978060272e-1}, {5, 6.02165389804559606850219397283e-2},
-     {6, -1.7578125e-2}},
-    {{1, 3.70920001185047927108779319836e-2}, {4, 1.70383925712239993810214054705e-1},
-     {5, 1.07262030446373284651809199168e-1}, {6, -1.53194377486244017527936158236e-2},
-     {7, 8.27378916381402288758473766002e-3}},
-    {{1, 6.24110958716075717114429577812e-1}, {4, -3.36089262944694129406857109825e0},
-     {5, -8.68219346841726006818189891453e-1}, {6, 2.75920996994467083049415600797e1},
-     {7, 2.01540675504778934086186788979e1}, {8, -4.34898841810699588477366255144e1}},
-    {{1, 4.77662536438264365890433908527e-1}, {4, -2.48811461997166764192642586468e0},
-     {5, -5.90290826836842996371446475743e-1}, {6, 2.12300514481811942347288949897e1},
-     {7, 1.52792336328824235832596922938e1}, {8, -3.32882109689848629194453265587e1},
-     {9, -2.03312017085086261358222928593e-2}},
-    {{1, -9.3714243008598732571704021658e-1}, {4, 5.18637242884406370830023853209e0},
-     {5, 1.09143734899672957818500254654e0}, {6, -8.14978701074692612513997267357e0},
-     {7, -1.85200656599969598641566180701e1}, {8, 2.27394870993505042818970056734e1},
-     {9, 2.49360555267965238987089396762e0}, {10, -3.0467644718982195003823669022e0}},
-    {{1, 2.27331014751653820792359768449e0}, {4, -1.05344954667372501984066689879e1},
-     {5, -2.00087205822486249909675718444e0}, {6, -1.79589318631187989172765950534e1},
-     {7, 2.79488845294199600508499808837e1}, {8, -2.85899827713502369474065508674e0},
-     {9, -8.87285693353062954433549289258e0}, {10, 1.23605671757943030647266201528e1},
-     {2, 6.43392746015763530355970484046e-1}},
-};
+#define EOB_DOPR_STAGES \
+{ \
+    {}, {}, \
+    {{1, 5.26001519587677318785587544488e-2}}, \
+    {{1, 1.97250569845378994544595329183e-2}, {2, 5.91751709536136983633785987549e-2}}, \
+    {{1, 2.95875854768068491816892993775e-2}, {3, 8.87627564304205475450678981324e-2}}, \
+    {{1, 2.41365134159266685502369798665e-1}, {3, -8.84549479328286085344864962717e-1}, \
+    {4, 9.24834003261792003115737966543e-1}}, \
+    {{1, 3.7037037037037037037037037037e-2}, {4, 1.70828608729473871279604482173e-1}, \
+    {5, 1.25467687566822425016691814123e-1}}, \
+    {{1, 3.7109375e-2}, {4, 1.70252211019544039314978060272e-1}, {5, 6.02165389804559606850219397283e-2}, \
+    {6, -1.7578125e-2}}, \
+    {{1, 3.70920001185047927108779319836e-2}, {4, 1.70383925712239993810214054705e-1}, \
+    {5, 1.07262030446373284651809199168e-1}, {6, -1.53194377486244017527936158236e-2}, \
+    {7, 8.27378916381402288758473766002e-3}}, \
+    {{1, 6.24110958716075717114429577812e-1}, {4, -3.36089262944694129406857109825e0}, \
+    {5, -8.68219346841726006818189891453e-1}, {6, 2.75920996994467083049415600797e1}, \
+    {7, 2.01540675504778934086186788979e1}, {8, -4.34898841810699588477366255144e1}}, \
+    {{1, 4.77662536438264365890433908527e-1}, {4, -2.48811461997166764192642586468e0}, \
+    {5, -5.90290826836842996371446475743e-1}, {6, 2.12300514481811942347288949897e1}, \
+    {7, 1.52792336328824235832596922938e1}, {8, -3.32882109689848629194453265587e1}, \
+    {9, -2.03312017085086261358222928593e-2}}, \
+    {{1, -9.3714243008598732571704021658e-1}, {4, 5.18637242884406370830023853209e0}, \
+    {5, 1.09143734899672957818500254654e0}, {6, -8.14978701074692612513997267357e0}, \
+    {7, -1.85200656599969598641566180701e1}, {8, 2.27394870993505042818970056734e1}, \
+    {9, 2.49360555267965238987089396762e0}, {10, -3.0467644718982195003823669022e0}}, \
+    {{1, 2.27331014751653820792359768449e0}, {4, -1.05344954667372501984066689879e1}, \
+    {5, -2.00087205822486249909675718444e0}, {6, -1.79589318631187989172765950534e1}, \
+    {7, 2.79488845294199600508499808837e1}, {8, -2.85899827713502369474065508674e0}, \
+    {9, -8.87285693353062954433549289258e0}, {10, 1.23605671757943030647266201528e1}, \
+    {2, 6.43392746015763530355970484046e-1}}, \
+    }
+__constant__ Term kStage[13][9] = EOB_DOPR_STAGES;
+constexpr Term kStageC[13][9] = EOB_DOPR_STAGES;
 __constant__ signed char kNTerms[13] = {0, 0, 1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9};
+constexpr int kNTermsC[13] = {0, 0, 1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9};
 __constant__ signed char kOutSlot[13] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 2, 3};
 
 constexpr double b1 = 5.42937341165687622380535766363e-2, b6 = 4.45031289275240888144113950566e0,
@@ -84,6 +88,44 @@ constexpr double er1 = 0.1312004499419488073250102996e-01, er6 = -0.122515644637
                  er9 = -0.3503288487499736816886487290e+00, er10 = 0.3341791187130174790297318841e+00,
                  er11 = 0.8192320648511571246570742613e-01, er12 = -0.2235530786388629525884427845e-01;
 constexpr double safe = 0.9, minscale = 1.0 / 3.0, maxscale = 6.0;
+
+// Running sums spread over the 32 lanes of a warp that carries one binary:
+// lane l holds component l & 3 of two sums, selected by its slot group
+// g = l >> 2: the argument sum of stage g + 2 (stages 2..9) and, for
+// g = 0, 1, 2, that of stage g + 10, or for g = 3, 4, 5 the increment sum
+// b_s k_s, the error sum er_s k_s and the correction sum -bhh_s k_s.  When
+// the slope of stage p exists, every lane adds its weights w[p][g][*] times
+// that slope (zero where stage p does not enter), so each sum is accumulated
+// in the reference's order (its term lists run over ascending stages) while
+// the lanes work on different sums in the same instruction.
+struct LaneWeights {
+    double w[13][8][2];
+};
+
+constexpr LaneWeights make_lane_weights()
+{
+    LaneWeights L{};
+    for (int s = 2; s <= 12; ++s) {
+        const int g = (s <= 9) ? s - 2 : s - 10, k = (s <= 9) ? 0 : 1;
+        for (int t = 0; t < kNTermsC[s]; ++t) {
+            const int slot = kStageC[s][t].slot;
+            const int p = (s == 12 && slot == 2) ? 11 : slot;  // stage 11 overwrote slot 2
+            L.w[p][g][k] = kStageC[s][t].a;
+        }
+    }
+    const double bw[13] = {0, b1, 0, 0, 0, 0, b6, b7, b8, b9, b10, b11, b12};
+    const double ew[13] = {0, er1, 0, 0, 0, 0, er6, er7, er8, er9, er10, er11, er12};
+    for (int p = 1; p <= 12; ++p) {
+        L.w[p][3][1] = bw[p];
+        L.w[p][4][1] = ew[p];
+    }
+    L.w[1][5][1] = -bhh1;
+    L.w[9][5][1] = -bhh2;
+    L.w[12][5][1] = -bhh3;
+    return L;
+}
+
+__device__ const LaneWeights kLaneW = make_lane_weights();
 }  // namespace dp
 
 // err^(-1/8) without pow(): a reciprocal square root and two square roots
@@ -131,45 +173,6 @@ struct IntArgs {
     long long max_tries;
 };
 
-// Stage sums with the slope slots fixed at compile time, for groups whose
-// lanes all work on the same stage (32 lanes or more per binary): the slopes
-// then stay in registers instead of local memory.
-__device__ __forceinline__ double stage_sum_fixed(int stage, const double (&kr)[11][1])
-{
-    switch (stage) {
-        case 2: return (0.0 + dp::kStage[2][0].a * kr[1][0]);
-        case 3: return ((0.0 + dp::kStage[3][0].a * kr[1][0]) + dp::kStage[3][1].a * kr[2][0]);
-        case 4: return ((0.0 + dp::kStage[4][0].a * kr[1][0]) + dp::kStage[4][1].a * kr[3][0]);
-        case 5: return (((0.0 + dp::kStage[5][0].a * kr[1][0]) + dp::kStage[5][1].a * kr[3][0]) + dp::kStage[5][2].a * kr[4][0]);
-        case 6: return (((0.0 + dp::kStage[6][0].a * kr[1][0]) + dp::kStage[6][1].a * kr[4][0]) + dp::kStage[6][2].a * kr[5][0]);
-        case 7: return ((((0.0 + dp::kStage[7][0].a * kr[1][0]) + dp::kStage[7][1].a * kr[4][0]) + dp::kStage[7][2].a * kr[5][0]) + dp::kStage[7][3].a * kr[6][0]);
-        case 8: return (((((0.0 + dp::kStage[8][0].a * kr[1][0]) + dp::kStage[8][1].a * kr[4][0]) + dp::kStage[8][2].a * kr[5][0]) + dp::kStage[8][3].a * kr[6][0]) + dp::kStage[8][4].a * kr[7][0]);
-        case 9: return ((((((0.0 + dp::kStage[9][0].a * kr[1][0]) + dp::kStage[9][1].a * kr[4][0]) + dp::kStage[9][2].a * kr[5][0]) + dp::kStage[9][3].a * kr[6][0]) + dp::kStage[9][4].a * kr[7][0]) + dp::kStage[9][5].a * kr[8][0]);
-        case 10: return (((((((0.0 + dp::kStage[10][0].a * kr[1][0]) + dp::kStage[10][1].a * kr[4][0]) + dp::kStage[10][2].a * kr[5][0]) + dp::kStage[10][3].a * kr[6][0]) + dp::kStage[10][4].a * kr[7][0]) + dp::kStage[10][5].a * kr[8][0]) + dp::kStage[10][6].a * kr[9][0]);
-        case 11: return ((((((((0.0 + dp::kStage[11][0].a * kr[1][0]) + dp::kStage[11][1].a * kr[4][0]) + dp::kStage[11][2].a * kr[5][0]) + dp::kStage[11][3].a * kr[6][0]) + dp::kStage[11][4].a * kr[7][0]) + dp::kStage[11][5].a * kr[8][0]) + dp::kStage[11][6].a * kr[9][0]) + dp::kStage[11][7].a * kr[10][0]);
-        case 12: return (((((((((0.0 + dp::kStage[12][0].a * kr[1][0]) + dp::kStage[12][1].a * kr[4][0]) + dp::kStage[12][2].a * kr[5][0]) + dp::kStage[12][3].a * kr[6][0]) + dp::kStage[12][4].a * kr[7][0]) + dp::kStage[12][5].a * kr[8][0]) + dp::kStage[12][6].a * kr[9][0]) + dp::kStage[12][7].a * kr[10][0]) + dp::kStage[12][8].a * kr[2][0]);
-        default: return 0.0;
-    }
-}
-
-__device__ __forceinline__ void store_slope_fixed(int stage, double (&kr)[11][1], double km)
-{
-    switch (stage) {
-        case 2: kr[2][0] = km; break;
-        case 3: kr[3][0] = km; break;
-        case 4: kr[4][0] = km; break;
-        case 5: kr[5][0] = km; break;
-        case 6: kr[6][0] = km; break;
-        case 7: kr[7][0] = km; break;
-        case 8: kr[8][0] = km; break;
-        case 9: kr[9][0] = km; break;
-        case 10: kr[10][0] = km; break;
-        case 11: kr[2][0] = km; break;
-        case 12: kr[3][0] = km; break;
-        default: break;
-    }
-}
-
 // component q of a 4-vector held in registers (selects, no local memory)
 __device__ __forceinline__ double pick4(const double v[4], int q)
 {
@@ -201,7 +204,8 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     constexpr int GW = kPair ? 32 : G;  // lanes of the group inside one warp
     constexpr bool kDist = (G >= 4);
     constexpr int NC = kDist ? 1 : 4;  // state components held by one lane
-    // every lane of a warp on the same stage: slopes in registers (stage_sum_fixed)
+    // every lane of a warp on the same stage: the stage sums spread over the
+    // lanes (dp::LaneWeights) instead of slopes in local memory
     constexpr bool kReg = (GW == 32);
     const int lane = threadIdx.x & 31;
     const int sub = lane & (GW - 1);
@@ -226,6 +230,10 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     // exists, so the end of a step is short (lanes of one warp reach it at
     // different iterations, and that code runs for the whole warp)
     double acc_b[NC], acc_e[NC], acc_h[NC];
+    // kReg: this lane's two running sums (slot group lane >> 2), its weights
+    // for the slope the coming right-hand side produces, its component of k1
+    double SA = 0.0, SB = 0.0, wA = 0.0, wB = 0.0, k1c = 0.0;
+    const int lg = lane >> 2;
     double x = 0.0, h = 0.0, hfix = 0.0, errOld = 1e-4;
     double om_hist[4] = {0.0, 0.0, 0.0, 0.0};  // omega of rows (step-4 .. step-1) % 4
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
@@ -292,7 +300,9 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
         int out_slot = 1;
         if (phase == kStage) {
             if constexpr (kReg) {
-                argl[0] = y[0] + h * stage_sum_fixed(stage, k);
+                const double sel = (stage <= 9) ? SA : SB;
+                const int src = (((stage <= 9) ? stage - 2 : stage - 10) << 2) | cq;
+                argl[0] = y[0] + h * __shfl_sync(0xffffffffu, sel, src);
             } else {
                 const int nt = dp::kNTerms[stage];
                 for (int c = 0; c < NC; ++c) {
@@ -308,6 +318,11 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             // idle lane: evaluate a harmless state of binary 0 (result unused)
             rec = &a.bins[0];
             for (int c = 0; c < NC; ++c) argl[c] = rec->y0[kDist ? cq : c];
+        }
+        if constexpr (kReg) {
+            const int p = (phase == kStage) ? stage : 1;
+            wA = dp::kLaneW.w[p][lg][0];
+            wB = dp::kLaneW.w[p][lg][1];
         }
         double arg[4];
         if constexpr (kDist) {
@@ -343,11 +358,17 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
 
         // ------------------------------------------------ advance the lane
         if (phase == kStartPass) {
-            for (int c = 0; c < NC; ++c) {
-                k[1][c] = km[c];
-                acc_b[c] = dp::b1 * km[c];
-                acc_e[c] = dp::er1 * km[c];
-                acc_h[c] = -dp::bhh1 * km[c];
+            if constexpr (kReg) {
+                k1c = km[0];
+                SA = wA * km[0];
+                SB = wB * km[0];
+            } else {
+                for (int c = 0; c < NC; ++c) {
+                    k[1][c] = km[c];
+                    acc_b[c] = dp::b1 * km[c];
+                    acc_e[c] = dp::er1 * km[c];
+                    acc_h[c] = -dp::bhh1 * km[c];
+                }
             }
             errOld = 1e-4;
             prevReject = false;
@@ -359,18 +380,28 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             continue;
         }
         if (phase == kStage) {
-            double wb, we, wh;
-            stage_weights(stage, &wb, &we, &wh);
-            if constexpr (kReg) store_slope_fixed(stage, k, km[0]);
-            for (int c = 0; c < NC; ++c) {
-                if constexpr (!kReg) k[out_slot][c] = km[c];
-                acc_b[c] = fma(wb, km[c], acc_b[c]);
-                acc_e[c] = fma(we, km[c], acc_e[c]);
-                acc_h[c] = fma(wh, km[c], acc_h[c]);
+            if constexpr (kReg) {
+                SA = fma(wA, km[0], SA);
+                SB = fma(wB, km[0], SB);
+            } else {
+                double wb, we, wh;
+                stage_weights(stage, &wb, &we, &wh);
+                for (int c = 0; c < NC; ++c) {
+                    k[out_slot][c] = km[c];
+                    acc_b[c] = fma(wb, km[c], acc_b[c]);
+                    acc_e[c] = fma(we, km[c], acc_e[c]);
+                    acc_h[c] = fma(wh, km[c], acc_h[c]);
+                }
             }
             if (stage < 12) {
                 ++stage;
                 continue;
+            }
+            if constexpr (kReg) {
+                // the increment, error and correction sums of this lane's component
+                acc_b[0] = __shfl_sync(0xffffffffu, SB, 12 | cq);
+                acc_e[0] = __shfl_sync(0xffffffffu, SB, 16 | cq);
+                acc_h[0] = __shfl_sync(0xffffffffu, SB, 20 | cq);
             }
             // error estimate (src/DOPR853.cu:537-618) from the running sums
             double e1 = 0.0, e2 = 0.0, ynew[NC];
@@ -447,10 +478,15 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 if (tries >= a.max_tries) { st |= EOB_ST_TRIES; end = true; }
                 if (!end) {
                     stage = 2;  // retry with the new h; k1 unchanged
-                    for (int c = 0; c < NC; ++c) {
-                        acc_b[c] = dp::b1 * k[1][c];
-                        acc_e[c] = dp::er1 * k[1][c];
-                        acc_h[c] = -dp::bhh1 * k[1][c];
+                    if constexpr (kReg) {
+                        SA = dp::kLaneW.w[1][lg][0] * k1c;
+                        SB = dp::kLaneW.w[1][lg][1] * k1c;
+                    } else {
+                        for (int c = 0; c < NC; ++c) {
+                            acc_b[c] = dp::b1 * k[1][c];
+                            acc_e[c] = dp::er1 * k[1][c];
+                            acc_h[c] = -dp::bhh1 * k[1][c];
+                        }
                     }
                     continue;
                 }
@@ -462,11 +498,17 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
         bool end_pass = false;
         if (phase == kStopTest) {
             // stopping rule on the accepted state (kk = f(y))
-            for (int c = 0; c < NC; ++c) {
-                k[1][c] = km[c];
-                acc_b[c] = dp::b1 * km[c];
-                acc_e[c] = dp::er1 * km[c];
-                acc_h[c] = -dp::bhh1 * km[c];
+            if constexpr (kReg) {
+                k1c = km[0];
+                SA = wA * km[0];
+                SB = wB * km[0];
+            } else {
+                for (int c = 0; c < NC; ++c) {
+                    k[1][c] = km[c];
+                    acc_b[c] = dp::b1 * km[c];
+                    acc_e[c] = dp::er1 * km[c];
+                    acc_h[c] = -dp::bhh1 * km[c];
+                }
             }
             const double r = arg[0], drdt = kk[0], omega = kk[1], dprdt = kk[2];  // arg = y here
             int code = 0;

@@ -350,6 +350,30 @@ EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
     return out;
 }
 
+// the log(r) polynomial itself (L, dL/du), without the factor log r: four
+// warps evaluate it beside log r and join the two afterwards (jet_join)
+EOB_HD Jet jet_poly_l(const HamJets &J, int j, double u)
+{
+    const double *l = J.l[j];
+    double lv = l[6], ld = 0.0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        ld = fma(ld, u, lv);
+        lv = fma(lv, u, l[k]);
+    }
+    return {lv, ld};
+}
+
+// a jet from its polynomial part p, sqrt(u) part s and log polynomial l:
+// value P + S + log(r) L, d/du = P' + S' - r L + log(r) L'
+EOB_HD Jet jet_join(const Jet &p, const Jet &s, const Jet &l, double lr, double r)
+{
+    Jet out;
+    out.v = fma(lr, l.v, p.v + s.v);
+    out.d = fma(lr, l.d, fma(-r, l.v, p.d + s.d));
+    return out;
+}
+
 // Sequential use of the same pieces (host tests, and one-lane callers)
 EOB_HD void ham_eval_jets(const HamJets &J, double r, double pr, double L, HamEval *out)
 {

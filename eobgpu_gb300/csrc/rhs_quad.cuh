@@ -4,7 +4,7 @@
 // binaries whose sequential chains set a batch's time:
 //
 //   stage           warp 0              warp 1              warp 2              warp 3
-//   jets            log r, log parts    polynomial parts    sqrt(u), sqrt parts --
+//   jets            log r               polynomial parts    sqrt(u), sqrt parts log polynomials
 //   combination a   1/Dc, A(u)          1/Dc, c(u)          B_np, q, W - L^2 c  N(u, p_r^2)
 //   combination b   even part sqrt(AW)  odd part            --                  y_2/y_3, 1/(8 pi nu)
 //   H, flux set-up  H and gradient,     m factors from      omega, v = omega    omega, log v,
@@ -24,7 +24,8 @@
 namespace eob {
 
 struct QuadXchg {
-    double jet[3][2][32];  // jets: [log, polynomial, sqrt part][v, d][lane]
+    double jet[3][2][32];  // jets: [log polynomial, polynomial, sqrt part][v, d][lane]
+    double lr;             // warp 0: log r
     double pa[2][32];      // warp 0: A, dA/du
     double pc[2][32];      // warp 1: c, dc/du
     double pw[3][32];      // warp 2: W - L^2 c and its u-derivative, dW/dp_r
@@ -53,23 +54,28 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
 
     // ---- jets (lanes 16..31 repeat lanes 0..15)
     if (q == 0) {
-        const Jet p = jet_part_l(J, j, u, r, eob_log(r));
-        x.jet[0][0][lane] = p.v;
-        x.jet[0][1][lane] = p.d;
+        const double lr = eob_log(r);
+        if (lane == 0) x.lr = lr;
     } else if (q == 1) {
         const Jet p = jet_half(J, j, false, u, r, 1.0);
         x.jet[1][0][lane] = p.v;
         x.jet[1][1][lane] = p.d;
     } else if (q == 2) {
-        const Jet p = jet_half(J, j, true, u, r, sqrt(u));
+        // sqrt(u) = 1/sqrt(r), independent of the division u = 1/r
+        const Jet p = jet_half(J, j, true, u, r, eob_rsqrt(r));
         x.jet[2][0][lane] = p.v;
         x.jet[2][1][lane] = p.d;
+    } else {
+        const Jet p = jet_poly_l(J, j, u);
+        x.jet[0][0][lane] = p.v;
+        x.jet[0][1][lane] = p.d;
     }
     pair_sync(ps);  // 1: jets
-    // poly + sqrt + log, in that order on every warp; each warp gathers only
-    // the jets its pieces read
-    const double jv = (x.jet[1][0][lane] + x.jet[2][0][lane]) + x.jet[0][0][lane];
-    const double jd = (x.jet[1][1][lane] + x.jet[2][1][lane]) + x.jet[0][1][lane];
+    // poly + sqrt + log r * log polynomial, the same expression on every
+    // warp; each warp gathers only the jets its pieces read
+    const Jet jn = jet_join({x.jet[1][0][lane], x.jet[1][1][lane]}, {x.jet[2][0][lane], x.jet[2][1][lane]},
+                            {x.jet[0][0][lane], x.jet[0][1][lane]}, x.lr, r);
+    const double jv = jn.v, jd = jn.d;
     Jet jt[kNumJets];
     auto gather = [&](int s) {
         jt[s].v = __shfl_sync(0xffffffffu, jv, s);

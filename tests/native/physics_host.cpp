@@ -73,6 +73,41 @@ void phys_ham_pair(const double *st, const double *add, int n, double *out)
     }
 }
 
+// the same through the pieces four warps evaluate: polynomial, sqrt(u) and
+// log-polynomial parts joined with log r (jet_join), then comb_A, comb_C,
+// comb_W, comb_N, the even and odd parts and comb_final
+void phys_ham_quad(const double *st, const double *add, int n, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        eob::HamCoeffs h;
+        eob::ham_coeffs_build(&h, add[i], add[n + i], add[2 * n + i], add[3 * n + i], add[5 * n + i], add[6 * n + i],
+                              add[7 * n + i], add[8 * n + i]);
+        eob::HamJets J;
+        eob::ham_jets_build(h, &J);
+        const double r = st[i], L = st[3 * n + i];
+        const double u = 1.0 / r, lr = eob::eob_log(r), su = eob::eob_rsqrt(r);
+        eob::Jet jt[eob::kNumJets];
+        for (int j = 0; j < eob::kNumJets; ++j)
+            jt[j] = eob::jet_join(eob::jet_half(J, j, false, u, r, 1.0), eob::jet_half(J, j, true, u, r, su),
+                                  eob::jet_poly_l(J, j, u), lr, r);
+        const double idc = 1.0 / jt[eob::J_DC].v;
+        double res[2][5];
+        for (int z = 0; z < 2; ++z) {
+            const double pr = z ? 0.0 : st[2 * n + i];
+            const eob::PartA a = eob::comb_A(jt, idc);
+            const eob::PartC c = eob::comb_C(J, jt, u, idc);
+            const eob::PartW w = eob::comb_W(jt, eob::comb_b(jt, pr * pr), pr);
+            const eob::PartN nn = eob::comb_N(J, jt, pr * pr);
+            const eob::HeffPart ev = eob::comb_even_parts(a, c, w, L);
+            const eob::HeffPart od = eob::comb_odd_parts(jt, u, idc, nn, pr, L);
+            const eob::HamPart hp = eob::comb_final(J, u, ev, od);
+            res[z][0] = hp.H; res[z][1] = hp.dHdr; res[z][2] = hp.dHdpr; res[z][3] = hp.dHdL; res[z][4] = hp.Hreal;
+        }
+        out[5 * i + 0] = res[0][0]; out[5 * i + 1] = res[0][1]; out[5 * i + 2] = res[0][2];
+        out[5 * i + 3] = res[0][3]; out[5 * i + 4] = res[1][3];
+    }
+}
+
 // flux as a warp pair sums it: multipoles at sorted positions 0..31 (one
 // warp) and 32..34 (the other), m factors per m, shared pieces from the two
 // cube roots

@@ -68,16 +68,19 @@ def test_ham_jets_match_ham_eval(phys, golden):
         assert np.max(np.abs(b[j][ok] - gr[q][ok]) / sc) < 1e-12
 
 
-def test_ham_pair_pieces_match_jets(phys, golden):
+@pytest.mark.parametrize("fn", ["phys_ham_pair", "phys_ham_quad"])
+def test_ham_pair_pieces_match_jets(phys, golden, fn):
     """The pieces two warps of a pair evaluate (jet halves and log part, the
-    combination in four parts) against the single-group jet evaluation."""
+    combination in four parts), and the pieces of four warps (log polynomials
+    joined with log r, the combination in finer parts), against the
+    single-group jet evaluation."""
     g = golden["ham_rhs"]
     st, add = np.ascontiguousarray(g["state"]), np.ascontiguousarray(g["add"])
     n = st.shape[1]
     a = np.zeros(5 * n)
     b = np.zeros(5 * n)
     phys.phys_ham_jets(dp(st), dp(add), ctypes.c_int(n), dp(a))
-    phys.phys_ham_pair(dp(st), dp(add), ctypes.c_int(n), dp(b))
+    getattr(phys, fn)(dp(st), dp(add), ctypes.c_int(n), dp(b))
     a, b = a.reshape(n, 5).T, b.reshape(n, 5).T
     ok = np.all(np.isfinite(a), axis=0)
     np.testing.assert_array_equal(np.all(np.isfinite(b), axis=0), ok)
