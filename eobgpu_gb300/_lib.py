@@ -53,6 +53,7 @@ _SIGS = {
     "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
     "eob_component_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
     "eob_pair_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
+    "eob_math_probe": (c_int, [_P, c_int, _P, _P]),
     "eob_noalloc_scratch_bytes": (c_size_t, []),
     "eob_waveform_lnl_noalloc": (c_int, [_P, c_int, _P, _P, c_int, c_double, _P, c_int, c_double,
                                          ctypes.POINTER(EobOptions), _P, _P, _P]),

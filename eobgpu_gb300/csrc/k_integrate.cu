@@ -128,8 +128,6 @@ constexpr LaneWeights make_lane_weights()
 __device__ const LaneWeights kLaneW = make_lane_weights();
 }  // namespace dp
 
-// err^(-1/8) without pow(): a reciprocal square root and two square roots
-__device__ __forceinline__ double inv_eighth_root(double x) { return sqrt(sqrt(rsqrt(x))); }
 
 __device__ __forceinline__ double pow4(double x)
 {
@@ -193,8 +191,8 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     // GB300 an FP64 instruction costs the same issue slot whatever the number
     // of active lanes).  The components are gathered by shuffles where the
     // right-hand side or the stopping rule needs all four; the error norm
-    // adds the four components in the reference's order, so every lane
-    // reaches the same accept/reject decision with the same bits.
+    // adds the four components by a butterfly that gives every lane the same
+    // bits, so all lanes reach the same accept/reject decision.
     //
     // G = 64 / 128: two / four warps per binary (rhs_pair.cuh, rhs_quad.cuh);
     // each warp runs the control state of a 32-lane group, role 0 writes the
@@ -235,7 +233,9 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     double SA = 0.0, SB = 0.0, wA = 0.0, wB = 0.0, k1c = 0.0;
     const int lg = lane >> 2;
     double x = 0.0, h = 0.0, hfix = 0.0, errOld = 1e-4;
-    double om_hist[4] = {0.0, 0.0, 0.0, 0.0};  // omega of rows (step-4 .. step-1) % 4
+    // omega at the last four stopping tests of this pass, newest first (zero
+    // before the pass's first row: the reference's omega array restarts per pass)
+    double om1 = 0.0, om2 = 0.0, om3 = 0.0, om4 = 0.0;
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
     bool prevReject = false, fix = false;
     long long tries = 0;
@@ -374,7 +374,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             prevReject = false;
             tries = 0;
             first_row = step + 1;
-            for (int q = 0; q < 4; ++q) om_hist[q] = 0.0;
+            om1 = om2 = om3 = om4 = 0.0;
             stage = 2;
             phase = kStage;
             continue;
@@ -409,21 +409,18 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 const double t = acc_b[c];
                 ynew[c] = y[c] + h * t;
                 const double mx = (y[c] > ynew[c]) ? y[c] : ynew[c];
-                const double sk = 1.0 / (a.atol + a.rtol * mx);
+                const double sk = eob_rcp(a.atol + a.rtol * mx);
                 e2 += pow4((t + acc_h[c]) * sk);
                 e1 += pow4(acc_e[c] * sk);
             }
             if constexpr (kDist) {
-                // the four components' terms summed in component order, as
-                // the reference's loop over the equations does
-                const double p1 = e1, p2 = e2;
-                e1 = __shfl_sync(gmask, p1, 0, GW);
-                e2 = __shfl_sync(gmask, p2, 0, GW);
-#pragma unroll
-                for (int q = 1; q < 4; ++q) {
-                    e1 += __shfl_sync(gmask, p1, q, GW);
-                    e2 += __shfl_sync(gmask, p2, q, GW);
-                }
+                // the four components' terms summed by a butterfly over the
+                // lanes that hold them, (t0 + t1) + (t2 + t3): addition
+                // commutes, so every lane gets the same bits
+                e1 += __shfl_xor_sync(gmask, e1, 1, GW);
+                e2 += __shfl_xor_sync(gmask, e2, 1, GW);
+                e1 += __shfl_xor_sync(gmask, e1, 2, GW);
+                e2 += __shfl_xor_sync(gmask, e2, 2, GW);
             }
             double denom = e1 + 0.01 * e2;
             denom = (denom < 0.0) ? 1.0 : denom;
@@ -436,7 +433,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 if (err == 0.0) {
                     scale = dp::maxscale;
                 } else {
-                    scale = dp::safe * inv_eighth_root(err);
+                    scale = dp::safe * eob_inv_eighth_root(err);
                     if (scale > dp::maxscale) scale = dp::maxscale;
                     else if (scale < dp::minscale) scale = dp::minscale;
                 }
@@ -449,7 +446,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 ok = true;
             } else {
                 prevReject = true;
-                double t = dp::safe * inv_eighth_root(err);
+                double t = dp::safe * eob_inv_eighth_root(err);
                 if (t < dp::minscale) t = dp::minscale; else if (t > 1e300) t = 1e300;
                 h = h * t;
                 ok = false;
@@ -517,13 +514,16 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             else if (r < 6.0 && dprdt > 0.0) code = 4;
             else if (step > 5) {
                 // history rows written in this pass, zero before (omega array restarts per pass)
-                double o[5];
-                for (int j = 1; j <= 4; ++j) o[j] = (step - j >= first_row) ? om_hist[(step - j) & 3] : 0.0;
-                const bool c2 = omega < o[1];
-                const bool c3 = (o[3] - o[4] < 0.0) && (o[2] - o[3] < 0.0) && (o[1] - o[2] < 0.0);
+                const bool c2 = omega < om1;
+                // the reference's differences om_j - om_(j+1) < 0, as comparisons
+                // (equal for finite values: a nonzero difference is exact in sign)
+                const bool c3 = (om3 < om4) && (om2 < om3) && (om1 < om2);
                 if (r < 6.0 && c2 && c3) code = 5;
             }
-            om_hist[step & 3] = omega;
+            om4 = om3;
+            om3 = om2;
+            om2 = om1;
+            om1 = omega;
             end_pass = (code != 0) || (x >= a.tmax) || (step >= a.cap - 1) || (tries >= a.max_tries);
             if (step >= a.cap - 1) st |= EOB_ST_MAXSTEP;
             if (tries >= a.max_tries && code == 0) st |= EOB_ST_TRIES;

@@ -131,6 +131,33 @@ extern "C" int eob_component_probe(const void *bins, int which, int iters, doubl
     return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 
+// The hot path's own reciprocal, reciprocal cube root, logarithm and
+// reciprocal square root next to the device library's, for accuracy tests:
+// out[8 i + 0..7] = eob_rcp, 1/x, eob_rcbrt, rcbrt, eob_log, log, eob_rsqrt,
+// eob_inv_eighth_root of x[i].
+__global__ void k_math_probe(const double *x, int n, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    double *o = out + 8 * (size_t)i;
+    o[0] = eob::eob_rcp(v);
+    o[1] = 1.0 / v;
+    o[2] = eob::eob_rcbrt(v);
+    o[3] = rcbrt(v);
+    o[4] = eob::eob_log(v);
+    o[5] = log(v);
+    o[6] = eob::eob_rsqrt(v);
+    o[7] = eob::eob_inv_eighth_root(v);
+}
+
+extern "C" int eob_math_probe(const double *x, int n, double *out, cudaStream_t stream)
+{
+    if (!x || !out || n < 1) return EOB_E_ARG;
+    k_math_probe<<<(n + 255) / 256, 256, 0, stream>>>(x, n, out);
+    return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
+}
+
 extern "C" int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream)
 {
     if (!out || blocks < 1 || threads < 1 || threads > 1024 || iters < 1) return EOB_E_ARG;

@@ -181,7 +181,7 @@ template <int m, class Tab>
 EOB_HD double flux_m(const Tab &t, const FluxShared &s, double Em, double hw, const double *vp2)
 {
     const double mx = m * s.x;
-    const double Tpre = mx / (1.0 - Em);  // (4 pi k)/(1 - exp(-4 pi k)), k = m H omega
+    const double Tpre = mx * eob_rcp(1.0 - Em);  // (4 pi k)/(1 - exp(-4 pi k)), k = m H omega
     const double km = m * hw;
     return flux_m_l<m, 1, Tab>(t, s, Tpre, 1.0, 4.0 * km * km, vp2);
 }
@@ -189,12 +189,14 @@ EOB_HD double flux_m(const Tab &t, const FluxShared &s, double Em, double hw, co
 // Radiation-reaction flux (before the division by nu of RR_force).
 // omega: orbital frequency in the flux (dH/dpphi at the state); Hreal = nu H;
 // omega_c: circular frequency (dH/dpphi at p_r = 0).
+// flux_sum() is the multipole sum S with flux = S omega^2 / (8 pi).
 template <class Tab>
-EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, double Hreal, double omega_c)
+EOB_HD double flux_sum(const Tab &t, double r, double pphi, double omega, double Hreal, double omega_c)
 {
     FluxShared s;
     s.omega = omega;
-    s.v = cbrt(omega);
+    const double ro = eob_rcbrt(omega);
+    s.v = omega * (ro * ro);  // omega^(1/3)
     s.lv = eob_log(s.v);
     // v_phi = r (omega_c^2 r^3)^(-1/3) omega = omega omega_c^(-2/3)
     (void)r;
@@ -223,7 +225,22 @@ EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, doubl
     sum += flux_m<6, Tab>(t, s, E6, hw, vp2);
     sum += flux_m<7, Tab>(t, s, E7, hw, vp2);
     sum += flux_m<8, Tab>(t, s, E8, hw, vp2);
-    return sum * omega * omega / (8.0 * kPi);
+    return sum;
+}
+
+template <class Tab>
+EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, double Hreal, double omega_c)
+{
+    return flux_sum(t, r, pphi, omega, Hreal, omega_c) * omega * omega / (8.0 * kPi);
+}
+
+// F / omega with F = flux / nu, from the multipole sum S: S omega / (8 pi nu)
+// = S omega inv2eta / (4 pi) -- the reference's flux / nu / omega
+// (src/EOB.cu:3046-3145) without its two divisions
+template <class Tab>
+EOB_HD double flux_over_omega(const Tab &t, double S, double omega)
+{
+    return (S * omega) * (t.c_inv2eta() * (0.25 / kPi));
 }
 
 // ODE right-hand side (src/EOB.cu:3046-3145): k = (dH/dpr, dH/dpphi,
@@ -234,11 +251,10 @@ EOB_HD void eob_rhs(const HamCoeffs &h, const Tab &t, const double y[4], double 
     HamEval e;
     ham_eval(h, y[0], y[2], y[3], &e);
     const double omega = e.dHdL;
-    const double flux = flux_eval(t, y[0], y[3], omega, e.Hreal, e.omega_c) / h.nu;
-    const double fo = flux / omega;
+    const double fo = flux_over_omega(t, flux_sum(t, y[0], y[3], omega, e.Hreal, e.omega_c), omega);
     k[0] = e.dHdpr;
     k[1] = omega;
-    k[2] = -e.dHdr - y[2] / y[3] * fo;
+    k[2] = -fma(y[2] * eob_rcp(y[3]), fo, e.dHdr);
     k[3] = -fo;
 }
 
@@ -253,19 +269,24 @@ EOB_HD void lm_of_index(int i, int *l, int *m)
 // Shared pieces of the lane-group flux from v = omega^(1/3) and
 // w = omega_c^(1/3): vPhi = r (omega_c^2 r^3)^(-1/3) omega = omega / w^2
 // (the reference's v_phi, src/EOB.cu:2610-2618, with the r's cancelled).
-EOB_HD FluxShared flux_shared_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+EOB_HD FluxShared flux_shared_make_rv(const FluxTable &t, double pphi, double omega, double Hreal, double v,
+                                      double vphi)
 {
     FluxShared s;
     s.omega = omega;
     s.v = v;
     s.lv = eob_log(v);
-    const double vphi = omega / (w * w);
     s.vphi2 = vphi * vphi;
     s.Se = fma(Hreal * Hreal - 1.0, t.inv2eta, 1.0);
     s.Sodd = v * pphi;
     s.x = 4.0 * kPi * Hreal * omega;
     s.E1 = exp(-s.x);
     return s;
+}
+
+EOB_HD FluxShared flux_shared_make(const FluxTable &t, double pphi, double omega, double Hreal, double v, double w)
+{
+    return flux_shared_make_rv(t, pphi, omega, Hreal, v, omega / (w * w));
 }
 
 // one multipole of the flux, l and m at run time: m^2 |h_lm|^2 / omega^2
@@ -318,7 +339,7 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
     if (m & 1) Em *= s.E1;
     if (m == 8) Em = e4 * e4;
     const double mx = m * s.x;
-    const double T2 = mx / (1.0 - Em) * P;
+    const double T2 = mx * eob_rcp(1.0 - Em) * P;
     return t.gmul[i] * T2 * (S * S) * (rpl * rpl) * vpw;
 }
 
@@ -357,7 +378,7 @@ EOB_HD const double *tprod_row(int l)
 
 // per-call pieces shared by every multipole of one lane group
 struct FluxLane {
-    double v, lv, v12, Se, Sodd;
+    double v, v2, lv, v12, Se, Sodd;
     double vp[8];  // vphi^(2 e), e = 2..9
     double S2e, S2o;  // Se^2, Sodd^2
 };
@@ -371,6 +392,7 @@ EOB_HD FluxLane flux_lane_make_rv(const FluxTable &t, double pphi, double omega,
     f.v = v;
     f.lv = lv;
     const double v2 = v * v, v4 = v2 * v2;
+    f.v2 = v2;
     f.v12 = v4 * v4 * v4;
     const double p1 = vphi * vphi;
     const double p2 = p1 * p1, p3 = p2 * p1, p4 = p2 * p2;
@@ -404,7 +426,7 @@ EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, do
 EOB_HD void flux_m_factors(int m, double x, double hw, double *T, double *k4)
 {
     const double xm = m * x;
-    *T = xm / (1.0 - exp(-xm));
+    *T = xm * eob_rcp(1.0 - exp(-xm));
     const double km = m * hw;
     *k4 = 4.0 * km * km;
 }
@@ -434,12 +456,30 @@ EOB_HD int lm_packed(int i)
 // (l!)^2 times (m x)/(1 - e^{-m x}) prod_{j<=l} (4 k^2 + j^2): the m factors).
 // KMAX bounds the rho_lm series of the modes evaluated together.
 // the series part without the v_phi power: S^2 (rho_lm^l + f_lm)^2
-template <int KMAX>
-EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
+// the series part from rho_lm's sum: S^2 (rho_lm^l + f_lm)^2 with the h22
+// calibration term
+EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, double rho)
 {
     const int lm = lm_packed(i);
     const int l = lm >> 4, m = lm & 15;
     const int eps = (l + m) & 1;
+    rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
+    // rho^l by squaring (l = 2..8)
+    const double r2 = rho * rho, r4 = r2 * r2;
+    double rpl = (l & 4) ? r4 : 1.0;
+    if (l & 2) rpl *= r2;
+    if (l & 1) rpl *= rho;
+    if (l == 8) rpl = r4 * r4;
+    const double aux = f.v * fma(t.f3[i], f.v2, t.f1[i]);
+    rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
+    const double S2 = eps ? f.S2o : f.S2e;
+    return S2 * (rpl * rpl);
+}
+
+template <int KMAX>
+EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
+{
+    const int m = lm_packed(i) & 15;
     const double elm = t.elog[m] + f.lv;
     // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
     double acc = t.rho[i][KMAX];
@@ -450,18 +490,22 @@ EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
         if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
         acc = fma(acc, f.v, ck);
     }
-    double rho = fma(acc, f.v, 1.0);
-    rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
-    // rho^l by squaring (l = 2..8)
-    const double r2 = rho * rho, r4 = r2 * r2;
-    double rpl = (l & 4) ? r4 : 1.0;
-    if (l & 2) rpl *= r2;
-    if (l & 1) rpl *= rho;
-    if (l == 8) rpl = r4 * r4;
-    const double aux = f.v * fma(t.f3[i], f.v * f.v, t.f1[i]);
-    rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
-    const double S2 = eps ? f.S2o : f.S2e;
-    return S2 * (rpl * rpl);
+    return flux_mode_s_rho(t, i, f, fma(acc, f.v, 1.0));
+}
+
+// rho_lm's series (degree <= 10) in two halves for two lanes: half 0 gives
+// c_1 + c_2 v + ... + c_5 v^4 and half 1 gives c_6 + c_7 v + ... + c_10 v^4,
+// c_k = rho_k + rhol_k eulerlog_m (rhol_k is zero where the series has no
+// log term); then rho = 1 + v (half 0 + v^5 half 1)
+EOB_HD double flux_rho_half(const FluxTable &t, int i, const FluxLane &f, int half)
+{
+    const int m = lm_packed(i) & 15;
+    const double elm = t.elog[m] + f.lv;
+    const double *rh = t.rho[i] + (half ? 6 : 1), *rl = t.rhol[i] + (half ? 6 : 1);
+    double acc = fma(rl[4], elm, rh[4]);
+#pragma unroll
+    for (int k = 3; k >= 0; --k) acc = fma(acc, f.v, fma(rl[k], elm, rh[k]));
+    return acc;
 }
 
 // vphi^(2 (l + eps)) of multipole i selected from the precomputed powers
@@ -585,25 +629,34 @@ __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const Flu
     }
 }
 
+// the multipole sum S (flux = S omega^2 / (8 pi)) over a group of G lanes
 template <int G>
-__device__ double flux_eval_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
+__device__ double flux_sum_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
 {
-    // cube roots of omega (even lanes) and omega_c (odd lanes) in one instruction
-    const double cr = cbrt((sub & 1) ? omega_c : omega);
-    const double v = __shfl_sync(0xffffffffu, cr, 0, G), w = __shfl_sync(0xffffffffu, cr, 1, G);
+    // reciprocal cube roots of omega (even lanes) and omega_c (odd lanes) in
+    // one instruction stream: v = omega r_omega^2, v_phi = omega r_c^2
+    const double rc = eob_rcbrt((sub & 1) ? omega_c : omega);
+    const double r0 = __shfl_sync(0xffffffffu, rc, 0, G), r1 = __shfl_sync(0xffffffffu, rc, 1, G);
+    const double v = omega * (r0 * r0), vphi = omega * (r1 * r1);
     double part;
     if constexpr (G >= 8) {
-        const FluxLane f = flux_lane_make(t, pphi, omega, Hreal, v, w);
+        const FluxLane f = flux_lane_make_rv(t, pphi, omega, Hreal, v, vphi, eob_log(v));
         double Tm, k4m;
         flux_m_factors((sub & 7) + 1, 4.0 * kPi * Hreal * omega, Hreal * omega, &Tm, &k4m);
         part = flux_rounds_lane<G, 0>(t, f, Tm, k4m, sub);
     } else {
-        const FluxShared s = flux_shared_make(t, pphi, omega, Hreal, v, w);
+        const FluxShared s = flux_shared_make_rv(t, pphi, omega, Hreal, v, vphi);
         part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-    return part * omega * omega / (8.0 * kPi);
+    return part;
+}
+
+template <int G>
+__device__ double flux_eval_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
+{
+    return flux_sum_group<G>(t, pphi, omega, Hreal, omega_c, sub) * omega * omega / (8.0 * kPi);
 }
 
 template <int G>
@@ -612,11 +665,10 @@ __device__ void eob_rhs_group(const HamJets &h, const FluxTable &t, const double
     HamEval e;
     ham_eval_group<G>(h, y[0], y[2], y[3], sub, &e);
     const double omega = e.dHdL;
-    const double flux = flux_eval_group<G>(t, y[3], omega, e.Hreal, e.omega_c, sub) / h.nu;
-    const double fo = flux / omega;
+    const double fo = flux_over_omega(t, flux_sum_group<G>(t, y[3], omega, e.Hreal, e.omega_c, sub), omega);
     k[0] = e.dHdpr;
     k[1] = omega;
-    k[2] = -e.dHdr - y[2] / y[3] * fo;
+    k[2] = -fma(y[2] * eob_rcp(y[3]), fo, e.dHdr);
     k[3] = -fo;
 }
 #endif

@@ -174,7 +174,7 @@ struct CombA {
 EOB_HD CombA comb_a(const HamJets &J, const Jet *jt, double u)
 {
     CombA o;
-    o.idc = 1.0 / jt[J_DC].v;
+    o.idc = eob_rcp(jt[J_DC].v);
     const PartA pa = comb_A(jt, o.idc);
     const PartC pc = comb_C(J, jt, u, o.idc);
     o.Av = pa.Av;
@@ -217,6 +217,25 @@ EOB_HD PartW comb_W(const Jet *jt, const CombB &b, double pr)
     o.Wu = fma(p2 * p2, b.qad, p2 * b.bnpd);
     o.Wp = 2.0 * pr * ((1.0 + b.bnpv) + p2 * fma(p2, fma(4.0 * p2, q8.v, 3.0 * q6.v), 2.0 * q4.v));
     return o;
+}
+
+// comb_W with dW/dp_r cut in two, for four warps: comb_W_b keeps its B_np
+// part 2 p_r (1 + B_np) and comb_Wp_q gives the rest,
+// 2 p_r p_r^2 (2 q_4 + 3 p_r^2 q_6 + 4 p_r^4 q_8), from the jets alone
+EOB_HD PartW comb_W_b(const CombB &b, double pr)
+{
+    const double p2 = pr * pr;
+    PartW o;
+    o.W = fma(p2 * p2, b.qa, fma(p2, 1.0 + b.bnpv, 1.0));
+    o.Wu = fma(p2 * p2, b.qad, p2 * b.bnpd);
+    o.Wp = 2.0 * pr * (1.0 + b.bnpv);
+    return o;
+}
+
+EOB_HD double comb_Wp_q(const Jet *jt, double pr)
+{
+    const double p2 = pr * pr;
+    return 2.0 * pr * (p2 * fma(p2, fma(4.0 * p2, jt[J_Q8].v, 3.0 * jt[J_Q6].v), 2.0 * jt[J_Q4].v));
 }
 
 // a piece of H_eff with its derivatives in u, p_r and L
@@ -329,12 +348,6 @@ EOB_HD Jet jet_half(const HamJets &J, int j, bool sq, double u, double r, double
     return out;
 }
 
-EOB_HD Jet jet_part_cs(const HamJets &J, int j, double u, double r, double su)
-{
-    const Jet a = jet_half(J, j, false, u, r, 1.0), b = jet_half(J, j, true, u, r, su);
-    return {a.v + b.v, a.d + b.d};
-}
-
 EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
 {
     const double *l = J.l[j];
@@ -351,7 +364,7 @@ EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
 }
 
 // the log(r) polynomial itself (L, dL/du), without the factor log r: four
-// warps evaluate it beside log r and join the two afterwards (jet_join)
+// warps evaluate it beside log r and join the pieces afterwards (jet_join_s)
 EOB_HD Jet jet_poly_l(const HamJets &J, int j, double u)
 {
     const double *l = J.l[j];
@@ -364,20 +377,34 @@ EOB_HD Jet jet_poly_l(const HamJets &J, int j, double u)
     return {lv, ld};
 }
 
-// a jet from its polynomial part p, sqrt(u) part s and log polynomial l:
-// value P + S + log(r) L, d/du = P' + S' - r L + log(r) L'
-EOB_HD Jet jet_join(const Jet &p, const Jet &s, const Jet &l, double lr, double r)
+// the sqrt(u) polynomial itself (S, dS/du), without the factor sqrt(u)
+EOB_HD Jet jet_poly_s(const HamJets &J, int j, double u)
+{
+    const double *c = J.s[j];
+    double sv = c[6], sd = 0.0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+        sd = fma(sd, u, sv);
+        sv = fma(sv, u, c[k]);
+    }
+    return {sv, sd};
+}
+
+// a jet from its polynomial part p, the sqrt(u) and log polynomials s and l,
+// su = sqrt(u), hs = r su / 2 = d sqrt(u) / du and lr = log r:
+// value P + su S + lr L, d/du = P' + su S' + hs S - r L + lr L'
+EOB_HD Jet jet_join_s(const Jet &p, const Jet &s, const Jet &l, double su, double hs, double lr, double r)
 {
     Jet out;
-    out.v = fma(lr, l.v, p.v + s.v);
-    out.d = fma(lr, l.d, fma(-r, l.v, p.d + s.d));
+    out.v = fma(lr, l.v, fma(su, s.v, p.v));
+    out.d = fma(lr, l.d, fma(-r, l.v, fma(hs, s.v, fma(su, s.d, p.d))));
     return out;
 }
 
 // Sequential use of the same pieces (host tests, and one-lane callers)
 EOB_HD void ham_eval_jets(const HamJets &J, double r, double pr, double L, HamEval *out)
 {
-    const double u = 1.0 / r, lr = eob_log(r), su = sqrt(u);
+    const double u = eob_rcp(r), lr = eob_log(r), su = eob_rsqrt(r);
     Jet jt[kNumJets];
     for (int j = 0; j < kNumJets; ++j) jt[j] = jet_eval(J, j, u, r, lr, su);
     const HamPart a = ham_combine(J, jt, u, pr, L);
@@ -399,7 +426,7 @@ __device__ __forceinline__ void ham_eval_group(const HamJets &J, double r, doubl
                                                HamEval *out)
 {
     static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0, "group size");
-    const double u = 1.0 / r, lr = eob_log(r), su = sqrt(u);
+    const double u = eob_rcp(r), lr = eob_log(r), su = eob_rsqrt(r);
     constexpr int R = (kNumJets + G - 1) / G;
     double mv[R], md[R];
 #pragma unroll

@@ -148,7 +148,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
 {
     const double r = y[0], L = y[3];
     const int j = lane & 15;
-    const double u = 1.0 / r;
+    const double u = eob_rcp(r);
 
     // ---- jets: role 0 the log(r) parts; role 1 the polynomial parts on
     // lanes 0..15 and the sqrt(u) parts on lanes 16..31
@@ -159,7 +159,8 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         x.jet[0][1][lane] = p.d;
     } else {
         const bool sq = lane >= 16;
-        const Jet hj = jet_half(J, j, sq, u, r, sq ? sqrt(u) : 1.0);
+        // sqrt(u) = 1/sqrt(r), independent of the division u = 1/r
+        const Jet hj = jet_half(J, j, sq, u, r, sq ? eob_rsqrt(r) : 1.0);
         const double ov = __shfl_xor_sync(0xffffffffu, hj.v, 16);
         const double od = __shfl_xor_sync(0xffffffffu, hj.d, 16);
         // lanes j and j + 16 hold the two halves; add them in one order
@@ -203,7 +204,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
             x.aux[1] = 1.0 / (8.0 * kPi * J.nu);
         }
         pair_sync(ps);  // 2
-        const HeffPart o = comb_odd(J, jt, u, 1.0 / jt[J_DC].v, pr, L);
+        const HeffPart o = comb_odd(J, jt, u, eob_rcp(jt[J_DC].v), pr, L);
         x.od[0][lane] = o.v;
         x.od[1][lane] = o.du;
         x.od[2][lane] = o.dp;
@@ -234,7 +235,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         // reciprocal cube roots of omega (even lanes) and omega_c (odd lanes)
         // in one instruction stream: v = omega r_omega^2 and
         // v_phi = omega / omega_c^(2/3) = omega r_c^2 without a division
-        const double rc = rcbrt((lane & 1) ? omega_c : omega);
+        const double rc = eob_rcbrt((lane & 1) ? omega_c : omega);
         const double r0 = __shfl_sync(0xffffffffu, rc, 0), r1 = __shfl_sync(0xffffffffu, rc, 1);
         FluxLane f = flux_lane_make_rv(t, L, omega, Hreal, omega * (r0 * r0), omega * (r1 * r1), 0.0);
         if (lane == 0) {
@@ -264,12 +265,13 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         // other warp, whose flux set-up is the longer of the two
         const double heff = x.ev[0][0] + x.od[0][0];
         const double s2 = fma(2.0 * J.nu, heff - 1.0, 1.0);
-        const double omega = J.M * eob_rsqrt(s2) * D;
+        const double omega = (J.M * D) * eob_rsqrt(s2);
         const double lv = eob_log(omega) * (1.0 / 3.0);
         if (lane == 0) x.fl[1] = lv;
         pair_sync(ps);  // 4
         FluxLane f;
         f.v = x.fl[0];
+        f.v2 = f.v * f.v;
         f.lv = x.fl[1];
         f.v12 = x.fl[2];
         f.Se = x.fl[3];
@@ -280,18 +282,19 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         for (int q = 0; q < 8; ++q) f.vp[q] = x.fl[5 + q];
         part = flux_warp_modes<32>(t, f, x, lane);
     }
+    // F / omega = total c1 with F = total omega^2 / (8 pi) / nu, and
+    // (y_2 / y_3) F / omega = total c2, beside the reduction
+    const double omega = x.ham[2];
+    const double c1 = omega * x.aux[1], c2 = x.aux[0] * c1;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
     if (lane == 0) x.part[role] = part;
     pair_sync(ps);  // 5: flux partial sums
     const double total = x.part[0] + x.part[1];
-    const double dHdr = x.ham[0], dHdpr = x.ham[1], omega = x.ham[2];
-    // F / omega with F = total omega^2 / (8 pi) / nu
-    const double fo = total * omega * x.aux[1];
-    k[0] = dHdpr;
+    k[0] = x.ham[1];
     k[1] = omega;
-    k[2] = -dHdr - x.aux[0] * fo;
-    k[3] = -fo;
+    k[2] = -fma(c2, total, x.ham[0]);
+    k[3] = -(total * c1);
 }
 
 }  // namespace eob

@@ -166,6 +166,12 @@ int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t
  * lanes, 7 Hamiltonian with 32 lanes, 8 right-hand side with 32 lanes. */
 int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
                         cudaStream_t stream);
+/* accuracy probe of the hot path's math (no reference counterpart): for each
+ * of the n device doubles x, out[8 i + 0..7] = the hot path's reciprocal, the
+ * device division 1/x, the hot path's x^(-1/3), the device rcbrt, the hot
+ * path's log, the device log, the hot path's 1/sqrt(x), the step controller's
+ * x^(-1/8); out: device, 8 n doubles */
+int eob_math_probe(const double *x, int n, double *out, cudaStream_t stream);
 /* warp-pair probes (no reference counterpart): which 0/1 = barrier round trip
  * (suspending / spinning wait, out int[blocks * 4]), 2 = the pair right-hand
  * side on binary 0 of `bins` (out double[blocks * 4]); threads a multiple of 64,

@@ -74,8 +74,8 @@ void phys_ham_pair(const double *st, const double *add, int n, double *out)
 }
 
 // the same through the pieces four warps evaluate: polynomial, sqrt(u) and
-// log-polynomial parts joined with log r (jet_join), then comb_A, comb_C,
-// comb_W, comb_N, the even and odd parts and comb_final
+// log polynomials joined with sqrt(u) and log r (jet_join_s), then comb_A, comb_C,
+// comb_W_b + comb_Wp_q, comb_N, the even and odd parts and comb_final
 void phys_ham_quad(const double *st, const double *add, int n, double *out)
 {
     for (int i = 0; i < n; ++i) {
@@ -88,15 +88,16 @@ void phys_ham_quad(const double *st, const double *add, int n, double *out)
         const double u = 1.0 / r, lr = eob::eob_log(r), su = eob::eob_rsqrt(r);
         eob::Jet jt[eob::kNumJets];
         for (int j = 0; j < eob::kNumJets; ++j)
-            jt[j] = eob::jet_join(eob::jet_half(J, j, false, u, r, 1.0), eob::jet_half(J, j, true, u, r, su),
-                                  eob::jet_poly_l(J, j, u), lr, r);
+            jt[j] = eob::jet_join_s(eob::jet_half(J, j, false, u, r, 1.0), eob::jet_poly_s(J, j, u),
+                                    eob::jet_poly_l(J, j, u), su, 0.5 * r * su, lr, r);
         const double idc = 1.0 / jt[eob::J_DC].v;
         double res[2][5];
         for (int z = 0; z < 2; ++z) {
             const double pr = z ? 0.0 : st[2 * n + i];
             const eob::PartA a = eob::comb_A(jt, idc);
             const eob::PartC c = eob::comb_C(J, jt, u, idc);
-            const eob::PartW w = eob::comb_W(jt, eob::comb_b(jt, pr * pr), pr);
+            eob::PartW w = eob::comb_W_b(eob::comb_b(jt, pr * pr), pr);
+            w.Wp = w.Wp + eob::comb_Wp_q(jt, pr);
             const eob::PartN nn = eob::comb_N(J, jt, pr * pr);
             const eob::HeffPart ev = eob::comb_even_parts(a, c, w, L);
             const eob::HeffPart od = eob::comb_odd_parts(jt, u, idc, nn, pr, L);
@@ -141,11 +142,22 @@ static double flux_quad_host(const eob::FluxTable &t, double pphi, double omega,
     double T[8], k4[8];
     for (int m = 1; m <= 8; ++m)
         eob::flux_m_factors(m, 4.0 * eob::kPi * Hreal * omega, Hreal * omega, &T[m - 1], &k4[m - 1]);
+    // sorted positions 0..15 from the two halves of rho's series, the rest whole
+    static const signed char order[35] = {0, 1, 4, 3, 2, 8, 7, 6, 5, 13, 11, 9, 12, 10, 19, 17, 15, 18,
+                                          16, 14, 26, 24, 22, 20, 25, 23, 21, 34, 33, 32, 31, 30, 29, 28, 27};
+    const double v5 = f.v2 * f.v2 * f.v;
     double sum = 0.0;
-    for (int i = 0; i < 35; ++i) {
+    for (int pos = 0; pos < 35; ++pos) {
+        const int i = order[pos];
         const int m = eob::lm_packed(i) & 15;
-        sum += (eob::flux_mode_b(t, i, T[m - 1], k4[m - 1]) * eob::flux_mode_vp_sq(i, vphi * vphi)) *
-               eob::flux_mode_s<10>(t, i, f);
+        double s;
+        if (pos < 16) {
+            const double lo = eob::flux_rho_half(t, i, f, 0), hi = eob::flux_rho_half(t, i, f, 1);
+            s = eob::flux_mode_s_rho(t, i, f, fma(fma(v5, hi, lo), f.v, 1.0));
+        } else {
+            s = eob::flux_mode_s<10>(t, i, f);
+        }
+        sum += (eob::flux_mode_b(t, i, T[m - 1], k4[m - 1]) * eob::flux_mode_vp_sq(i, vphi * vphi)) * s;
     }
     return sum * omega * omega / (8.0 * eob::kPi);
 }
