@@ -233,6 +233,7 @@ def config_block(cfg, args, extra=None):
          "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12, "queue": "longest first",
          "l2": "flushed between timed steps (256 MiB write)",
          "lanes_per_binary": getattr(args, "lanes", 0) or "auto",
+         "head_quads": "auto" if getattr(args, "head_quads", -1) < 0 else args.head_quads,
          "integrator_block": getattr(args, "block", 0) or "default", "integrator_grid": getattr(args, "grid", 0) or "auto"}
     if extra:
         d.update(extra)
@@ -438,7 +439,7 @@ def run_serving(args, ws, rank, local):
     lanes = args.lanes or 8
     classes = [(1500, 1024, 2), (args.max_steps, 512, 1)]
     server = LikelihoodServer(data, cfg.dt, amp, classes=classes, lanes_per_binary=lanes,
-                              precision=0 if args.fp64 else 1, device=device)
+                              precision=0 if args.fp64 else 1, head_quads=args.head_quads, device=device)
     trace = workload.serving_trace(args.requests, 1.0, stream=rank)
     for _ in range(args.warmup):
         server.evaluate(trace.params[0])
@@ -469,6 +470,7 @@ def run_serving(args, ws, rank, local):
                            "offered_load": "70 % of the measured capacity", "classes_max_steps_batch_slots": classes,
                            "admission": "by estimated trajectory rows (chirp-time fit x3), re-run on overflow",
                            "requeued": int(sum(r["requeued"] for r in results)), "lanes_per_binary": lanes,
+                           "head_quads": "auto" if args.head_quads < 0 else args.head_quads,
                            "max_steps": args.max_steps, "dt_s": cfg.dt, "n_samples": cfg.n_samples,
                            "l2": "inputs of each batch are new; no flush (latency run)"},
                 "e2e": {"value": value, "unit": "evals/s",
@@ -509,6 +511,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=96)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="integrator lanes per binary (0: chosen from the batch size)")
+    ap.add_argument("--head-quads", type=int, default=-1,
+                    help="longest binaries on four warps each beside groups of 8..64 lanes (-1: the library's choice)")
     ap.add_argument("--block", type=int, default=0, help="integrator threads per block (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="integrator blocks (0: one wave of resident blocks)")
     ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl"],
@@ -552,6 +556,7 @@ def main():
     from eobgpu_gb300 import _lib
     opt = _lib.default_options()
     opt.lanes_per_binary = args.lanes
+    opt.head_quads = args.head_quads
     opt.block = args.block
     opt.grid = args.grid
     mixed = args.config == 3 and not args.fp64
@@ -698,7 +703,8 @@ def main():
         extra_cfg["chunks"] = chunked.info(B)
     if chunked is None and tuned is not None:
         extra_cfg["autotune"] = {"lanes_per_binary": tuned.lanes_per_binary, "block": tuned.block,
-                                 "spline_series_per_block": tuned.spline_series_per_block, "table": tuned.table}
+                                 "spline_series_per_block": tuned.spline_series_per_block,
+                                 "head_quads": tuned.head_quads, "table": tuned.table}
     line = None
     if rank == 0:
         cpu_base = None

@@ -42,12 +42,14 @@ class TuneResult:
     spline_series_per_block: int
     ms: float
     table: list
+    head_quads: int = -1
 
     def options(self, base: _lib.EobOptions | None = None) -> _lib.EobOptions:
         o = _lib.default_options() if base is None else base
         o.lanes_per_binary = self.lanes_per_binary
         o.block = self.block
         o.spline_tile = self.spline_series_per_block
+        o.head_quads = self.head_quads
         return o
 
 
@@ -63,11 +65,13 @@ def _time(wl, P, D, dt, amp, order, reps):
 
 
 def tune(params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, modes=((2, 2),), max_steps: int = 6000,
-         lanes=(1, 2, 4, 8, 16, 32, 64, 128), blocks=(64, 128, 256), spline_tiles=(1, 4), reps: int = 1,
-         cache_file: str | None = None, base: _lib.EobOptions | None = None) -> TuneResult:
+         lanes=(1, 2, 4, 8, 16, 32, 64, 128), blocks=(64, 128, 256), spline_tiles=(1, 4), heads=(16, 32, 64),
+         reps: int = 1, cache_file: str | None = None, base: _lib.EobOptions | None = None) -> TuneResult:
     """Time every candidate on this batch and return the fastest.  The lanes
-    per binary are searched first (block 128); the block size only for the
-    best lane count; the spline tile last."""
+    per binary are searched first (block 128, the library's head choice),
+    then a head of the longest binaries on four warps beside groups of 8..64
+    lanes near the best count; the block size only for the best lane count
+    (without a head); the spline tile last."""
     key = signature(params, len(modes), int(data.shape[0]), max_steps)
     if key in _CACHE:
         return _CACHE[key]
@@ -82,23 +86,38 @@ def tune(params: torch.Tensor, data: torch.Tensor, dt: float, amp: float, modes=
     order = longest_first(params)
     table = []
 
-    def run(g, bs, tile):
+    def run(g, bs, tile, head=-1):
         o = _lib.default_options() if base is None else base
-        o.lanes_per_binary, o.block, o.spline_tile = g, bs, tile
+        o.lanes_per_binary, o.block, o.spline_tile, o.head_quads = g, bs, tile, head
         wl = WaveformLikelihood(B, max_steps, list(modes), int(data.shape[0]), device=params.device, options=o)
         ms = _time(wl, params, data, dt, amp, order, reps)
-        table.append({"lanes_per_binary": g, "block": bs, "spline_series_per_block": tile, "ms": ms})
+        table.append({"lanes_per_binary": g, "block": bs, "spline_series_per_block": tile, "head_quads": head,
+                      "ms": ms})
         del wl
         return ms
 
     best_g = min(lanes, key=lambda g: run(g, 128, spline_tiles[0]))
-    best_bs = min(blocks, key=lambda bs: run(best_g, bs, spline_tiles[0]) if bs != 128 else
-                  next(t["ms"] for t in table if t["lanes_per_binary"] == best_g and t["block"] == 128))
-    best_tile = min(spline_tiles, key=lambda t: run(best_g, best_bs, t) if t != spline_tiles[0] else
-                    min(e["ms"] for e in table if e["lanes_per_binary"] == best_g and e["block"] == best_bs))
+    best_head = -1
+    best_ms = min(e["ms"] for e in table if e["lanes_per_binary"] == best_g)
+    for g in sorted({g for g in (best_g // 2, best_g, best_g * 2, 64) if g in (8, 16, 32, 64)}):
+        for h in heads:
+            if h >= B:
+                continue
+            ms = run(g, 128, spline_tiles[0], h)
+            if ms < best_ms:
+                best_ms, best_g, best_head = ms, g, h
+    if best_head == -1:
+        best_bs = min(blocks, key=lambda bs: run(best_g, bs, spline_tiles[0]) if bs != 128 else
+                      min(t["ms"] for t in table if t["lanes_per_binary"] == best_g and t["block"] == 128
+                          and t["head_quads"] == -1))
+    else:
+        best_bs = 128  # the launch with a head has its own block shape
+    best_tile = min(spline_tiles, key=lambda t: run(best_g, best_bs, t, best_head) if t != spline_tiles[0] else
+                    min(e["ms"] for e in table if e["lanes_per_binary"] == best_g and e["block"] == best_bs
+                        and e["head_quads"] == best_head))
     ms = min(e["ms"] for e in table if e["lanes_per_binary"] == best_g and e["block"] == best_bs
-             and e["spline_series_per_block"] == best_tile)
-    r = TuneResult(best_g, best_bs, best_tile, ms, table)
+             and e["spline_series_per_block"] == best_tile and e["head_quads"] == best_head)
+    r = TuneResult(best_g, best_bs, best_tile, ms, table, best_head)
     _CACHE[key] = r
     if cache_file:
         disk = {}

@@ -613,10 +613,12 @@ __global__ void __launch_bounds__(256, 1) k_integrate_pair(IntArgs a)
     integrate_body<64>(a, xch, bars);
 }
 
-// The longest binaries on four warps, the rest on warp pairs, in one launch
-// of 128-thread blocks: blocks [0, nq) first run four-warp groups over the
-// first `head` binaries of the order (their own queue counter, queue[7]),
-// then join the other blocks as two pairs over the remaining binaries.
+// The longest binaries on four warps, the rest on groups of GB lanes (warp
+// pairs for GB = 64), in one launch of 128-thread blocks: blocks [0, nq)
+// first run four-warp groups over the first `head` binaries of the order
+// (their own queue counter, queue[7]), then join the other blocks over the
+// remaining binaries.
+template <int GB>
 __global__ void __launch_bounds__(128, 1) k_integrate_mixed(IntArgs a, int nq, int head)
 {
     __shared__ QuadXchg xq;
@@ -641,7 +643,8 @@ __global__ void __launch_bounds__(128, 1) k_integrate_mixed(IntArgs a, int nq, i
     IntArgs ap = a;
     ap.base = a.base + head;
     ap.B = a.B - head;
-    integrate_body<64>(ap, xp, bp);
+    if constexpr (GB == 64) integrate_body<64>(ap, xp, bp);
+    else integrate_body<GB>(ap, (PairXchg *)nullptr, nullptr);
 }
 
 // warp quads: blockDim.x a multiple of 128, at most kQuadMax quads
@@ -745,24 +748,31 @@ cudaError_t launch_integrate(const Ws &w, const RunArgs &ra, cudaStream_t s)
     a.base = 0;
     cudaError_t e = cudaMemsetAsync(w.queue, 0, sizeof(unsigned long long) * 8, s);
     if (e != cudaSuccess) return e;
-    // warp pairs with a head on four warps
-    if (G == 64 && ra.opt.head_quads != 0) {
+    // a head of the longest binaries on four warps, the rest on warp pairs
+    // (automatic: the 16 longest, at most B / 64) or, when asked for, on
+    // lane groups of 8 .. 32
+    if ((G == 64 || (G >= 8 && G <= 32)) && ra.opt.head_quads != 0) {
         int dev = 0, nsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         int head = ra.opt.head_quads;
-        if (head < 0) head = (ra.B >= 64) ? (ra.B / 64 < 16 ? ra.B / 64 : 16) : 0;
+        if (head < 0) head = (G == 64 && ra.B >= 64) ? (ra.B / 64 < 16 ? ra.B / 64 : 16) : 0;
         if (head > ra.B) head = ra.B;
         if (head > 0) {
-            static bool carve = false;
-            if (!carve) {
-                cudaFuncSetAttribute(k_integrate_mixed, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-                carve = true;
+            void (*kern)(IntArgs, int, int) = G == 64 ? k_integrate_mixed<64>
+                                              : G == 32 ? k_integrate_mixed<32>
+                                              : G == 16 ? k_integrate_mixed<16>
+                                                        : k_integrate_mixed<8>;
+            static bool carve[4] = {false, false, false, false};
+            const int ci = G == 64 ? 0 : G == 32 ? 1 : G == 16 ? 2 : 3;
+            if (!carve[ci]) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+                carve[ci] = true;
             }
             const int nq = head < nsm ? head : nsm;
-            const long long need = nq + ((long long)(ra.B - head) * 64 + 127) / 128;
+            const long long need = nq + ((long long)(ra.B - head) * G + 127) / 128;
             const int grid = (int)(need < nsm ? need : nsm);
-            k_integrate_mixed<<<grid > nq ? grid : nq, 128, 0, s>>>(a, nq, head);
+            kern<<<grid > nq ? grid : nq, 128, 0, s>>>(a, nq, head);
             return cudaGetLastError();
         }
     }

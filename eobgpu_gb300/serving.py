@@ -128,7 +128,7 @@ class LikelihoodServer:
 
     def __init__(self, data, dt: float, amp: float, modes=((2, 2),), max_batch: int = 512, max_steps: int = 4000,
                  slots: int = 2, lanes_per_binary: int = 8, hbm_budget_bytes: int | None = None, classes=None,
-                 row_safety: float = 3.0, precision: int = 0, device="cuda"):
+                 row_safety: float = 3.0, precision: int = 0, head_quads: int = -1, device="cuda"):
         if not torch.cuda.is_available():
             raise _lib.EOBError("no CUDA device: the EOB path runs only on the GPU")
         self.device = torch.device(device)
@@ -154,6 +154,7 @@ class LikelihoodServer:
         opts = _lib.default_options()
         opts.lanes_per_binary = int(lanes_per_binary)
         opts.precision = int(precision)
+        opts.head_quads = int(head_quads)
         self.slots = []
         for ci, ((L, b, _), cnt) in enumerate(zip(classes, counts)):
             for _ in range(cnt):

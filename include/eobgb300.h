@@ -54,8 +54,10 @@ typedef struct eob_options {
                                sub-partitions) or 128 (four warps, one per sub-partition of an SM);
                                0 = chosen from the batch size */
     int spline_tile;        /* spline build: series (one warp each) per block, 1..8 (0 = default 4) */
-    int head_quads;         /* with warp pairs: the head_quads longest binaries (first in `order`) on four
-                               warps each, concurrently with the pairs (-1 = chosen from the batch, 0 = none) */
+    int head_quads;         /* with warp pairs or groups of 8, 16 or 32 lanes: the head_quads longest
+                               binaries (first in `order`) on four warps each, concurrently with the rest
+                               (-1 = chosen from the batch: with warp pairs min(B / 64, 16), otherwise
+                               none; 0 = none) */
 } eob_options;
 
 void eob_options_default(eob_options *o);

@@ -141,10 +141,12 @@ def test_config1_lanes_per_binary(torch_cuda, golden, G):
     np.testing.assert_array_equal(nsteps, c["nsteps"])
 
 
-def test_config1_mixed_head(torch_cuda, golden):
-    """Warp pairs with the longest binaries on four warps in the same launch
-    (eob_options.head_quads): the reference's lnL and row counts, and the same
-    bits as each group size run alone for its binaries."""
+@pytest.mark.parametrize("bulk", [64, 8, 32])
+def test_config1_mixed_head(torch_cuda, golden, bulk):
+    """Warp pairs (or lane groups of 8 and 32) with the longest binaries on
+    four warps in the same launch (eob_options.head_quads): the reference's
+    lnL and row counts, and the same bits as each group size run alone for
+    its binaries."""
     torch = torch_cuda
     from eobgpu_gb300 import _lib
     from eobgpu_gb300.pipeline import WaveformLikelihood, longest_first
@@ -153,7 +155,7 @@ def test_config1_mixed_head(torch_cuda, golden):
     D = torch.tensor(c["data"], device="cuda")
     order = longest_first(P)
     runs = {}
-    for name, G, head in (("mixed", 64, 3), ("pairs", 64, 0), ("quads", 128, 0)):
+    for name, G, head in (("mixed", bulk, 3), ("pairs", bulk, 0), ("quads", 128, 0)):
         opt = _lib.default_options()
         opt.lanes_per_binary = G
         opt.head_quads = head
