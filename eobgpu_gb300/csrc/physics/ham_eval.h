@@ -40,8 +40,9 @@ EOB_HD double eob_rsqrt(double x)
 // references over 10^6 arguments in [1e-6, 1e6]: within 0.51 and 0.77 ulp.
 // Arguments are finite, nonzero and of normal range on the hot path (r >= 1,
 // D_c ~ 1, 1 - e^(-m x) in (0, 1), omega in (0, 1)); x = 0 or x = inf give
-// NaN, which the integrator's finiteness checks report.  Host: 1/x and
-// 1/cbrt(x).
+// NaN, which the integrator's finiteness checks report, and the cube root's
+// single-precision seed needs |x| within the float range (1e-38 .. 3e38;
+// orbital frequencies are above 1e-6).  Host: 1/x and 1/cbrt(x).
 EOB_HD double eob_rcp(double x)
 {
 #ifdef __CUDA_ARCH__
