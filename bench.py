@@ -186,6 +186,70 @@ def cpu_time(params, cfg, data, amp, max_step, cores):
     return t1 - t0, np.array(out)
 
 
+def _oracle_detail_worker(args):
+    p, dt, N, modes, data, amp, max_step = args
+    from oracle.oracle import Oracle
+    r = Oracle().lnl_one(p, dt, N, modes, data, amp, max_step=max_step, want_detail=True)
+    return r["lnl"], r["status"], r["h"], r["npts"]
+
+
+def accuracy_vs_oracle(params, cfg, data, amp, max_steps, precision, device, sample, cores):
+    """Waveform and lnL error of the GPU path against the FP64 oracle on an
+    evenly spread sample of the batch (outside any timed region): phase and
+    relative amplitude at the oracle's amplitude peak, mismatch
+    1 - Re<a, c> / (|a| |c|) over the N samples, |dlnL| and |dlnL| / |lnL|.
+    Binaries whose template ends on another sample than the oracle's (the
+    two samplings of the trajectory stop on different sides of a sample
+    time; the last sample, at the merger, then carries h^2 ~ 25-50 of lnL)
+    are counted apart and their worst values reported separately."""
+    import multiprocessing as mp
+    import torch
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    idx = np.unique(np.linspace(0, len(params) - 1, min(sample, len(params))).astype(int))
+    P = np.ascontiguousarray(params[idx])
+    N = int(len(data))
+    o = _lib.default_options()
+    o.precision = precision
+    wl = WaveformLikelihood(len(P), max_steps, list(cfg.modes), N, device=device, options=o)
+    Pd = torch.tensor(P, device=device)
+    lnl, st = wl.run(Pd, torch.tensor(data, device=device), cfg.dt, amp)
+    hs, _ = wl.strain(Pd, cfg.dt, N)
+    lnl, st, hs = lnl.cpu().numpy(), st.cpu().numpy(), hs.cpu().numpy()
+    npts = wl.npts()
+    del wl, Pd
+    torch.cuda.empty_cache()
+    jobs = [(p, cfg.dt, N, list(cfg.modes), data, amp, max_steps) for p in P]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_oracle_detail_worker, jobs, chunksize=1)
+    m = {True: [], False: []}  # same end sample as the oracle: metrics
+    skipped = 0
+    for b, (ol, ost, a, onp) in enumerate(res):
+        if ost != 0 or st[b] != 0:
+            skipped += 1
+            continue
+        c = hs[b]
+        ov = np.real(np.vdot(a, c)) / np.sqrt(np.real(np.vdot(a, a)) * np.real(np.vdot(c, c)))
+        k = int(np.argmax(np.abs(a)))
+        m[int(npts[b]) == int(onp)].append((
+            abs((np.angle(c[k]) - np.angle(a[k]) + np.pi) % (2 * np.pi) - np.pi), abs(abs(c[k]) / abs(a[k]) - 1),
+            1 - ov, abs(lnl[b] - ol), abs(lnl[b] - ol) / abs(ol)))
+    same = np.array(m[True]).reshape(-1, 5)
+    flip = np.array(m[False]).reshape(-1, 5)
+    out = {"vs": "FP64 oracle (CPU restatement, pinned to the reference's own code)",
+           "precision": "mixed" if precision else "f64", "sample": len(P), "skipped_status": skipped,
+           "same_end_sample": len(same), "end_sample_differs": len(flip)}
+    if len(same):
+        out.update({"max_dphi_at_peak_rad": float(same[:, 0].max()), "max_rel_amp_at_peak": float(same[:, 1].max()),
+                    "max_mismatch": float(same[:, 2].max()), "max_abs_dlnl": float(same[:, 3].max()),
+                    "max_rel_dlnl": float(same[:, 4].max()), "median_rel_dlnl": float(np.median(same[:, 4])),
+                    "frac_rel_dlnl_le_1e-9": float(np.mean(same[:, 4] <= 1e-9))})
+    if len(flip):
+        out["end_sample_differs_worst"] = {"max_mismatch": float(flip[:, 2].max()),
+                                           "max_abs_dlnl": float(flip[:, 3].max())}
+    return out
+
+
 def cpu_sample(params, n):
     """Deterministic bounded sample: every k-th binary."""
     step = max(1, len(params) // n)
@@ -459,6 +523,11 @@ def run_serving(args, ws, rank, local):
     lat = np.concatenate([r["latency_s"] for r in results])
     ok = all(np.all(st == 0) for r in results for st in r["status"])
     if rank == 0:
+        accuracy = None
+        if args.accuracy_sample > 0:
+            allp = np.concatenate([np.atleast_2d(p) for p in trace.params])
+            accuracy = accuracy_vs_oracle(allp, cfg, data, amp, args.max_steps, 0 if args.fp64 else 1, device,
+                                          args.accuracy_sample, os.cpu_count() or 1)
         value = nbin / wall
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
@@ -483,7 +552,8 @@ def run_serving(args, ws, rank, local):
                              "slot_busy_fraction": sat["slot_busy_fraction"]},
                 "batches": int(sum(r["batches"] for r in results)),
                 "gpu_launches": int(8 * sum(r["batches"] for r in results)),
-                "roofline": None, "cpu_baseline": None, "clocks": clocks, "status_ok": bool(ok)}
+                "roofline": None, "cpu_baseline": None, "clocks": clocks, "status_ok": bool(ok),
+                "accuracy": accuracy}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
@@ -509,6 +579,9 @@ def main():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--max-steps", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=96)
+    ap.add_argument("--accuracy-sample", type=int, default=-1,
+                    help="binaries compared with the FP64 oracle after the timing (-1: 64, or 256 for "
+                         "configuration 5; 0: none)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="integrator lanes per binary (0: chosen from the batch size)")
     ap.add_argument("--head-quads", type=int, default=-1,
@@ -526,6 +599,8 @@ def main():
     if not args.max_steps:
         args.max_steps = {1: 4000, 2: 6000, 3: 4000, 4: 4000, 5: 16000}[args.config]
     args.warmup = max(3, args.warmup)
+    if args.accuracy_sample < 0:
+        args.accuracy_sample = 256 if args.config == 5 else 64
     if args.census:
         census(args)
         return
@@ -559,7 +634,7 @@ def main():
     opt.head_quads = args.head_quads
     opt.block = args.block
     opt.grid = args.grid
-    mixed = args.config == 3 and not args.fp64
+    mixed = args.config in (3, 5) and not args.fp64
     opt.precision = 1 if mixed else 0
     P = torch.tensor(params, device=device)
     D = torch.tensor(data, device=device)
@@ -707,6 +782,13 @@ def main():
                                  "head_quads": tuned.head_quads, "table": tuned.table}
     line = None
     if rank == 0:
+        accuracy = None
+        if args.accuracy_sample > 0:
+            if chunked is not None:
+                del chunked, wl, run_any
+            torch.cuda.empty_cache()
+            accuracy = accuracy_vs_oracle(params, cfg, data, amp, args.max_steps, 1 if mixed else 0, device,
+                                          args.accuracy_sample, os.cpu_count() or 1)
         cpu_base = None
         if not args.no_cpu_baseline:
             cores = os.cpu_count() or 1
@@ -732,7 +814,7 @@ def main():
                 "status_ok": int(np.sum(status == 0)),
                 "status_other": {str(int(v)): int(c) for v, c in zip(*np.unique(status[status != 0],
                                                                                   return_counts=True))},
-                "rows": cnt["rows"]}
+                "rows": cnt["rows"], "accuracy": accuracy}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
