@@ -244,6 +244,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     const BinaryRec *rec = nullptr;
     double *tr = nullptr;
     bool queue_empty = false;
+    int cyc = 0;  // iterations of this warp (the same on every lane)
 
     for (;;) {
         // ------------------------------------------------ bookkeeping
@@ -289,9 +290,24 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 phase = kStartPass;
             }
         }
-        const bool active = (phase != kIdle);
+        const bool live = (phase != kIdle);
         // all lanes of the warp idle and the queue exhausted: done
-        if (__all_sync(0xffffffffu, !active)) break;
+        if (__all_sync(0xffffffffu, !live)) break;
+        // Several binaries per warp keep their steps in phase: a step starts
+        // (stage 2) only at iteration 0 of the warp's 12-iteration cycle and
+        // a pass (its first slope) only at iteration 11, so the end-of-step
+        // and stopping blocks, which the whole warp issues whenever any lane
+        // needs them, run once per cycle instead of nearly every iteration.
+        // A lane that would start off-cycle waits (its right-hand side is
+        // evaluated at its own state and discarded): about six iterations
+        // per pass and one per rejected step.
+        bool wait = false;
+        if constexpr (!kReg) {
+            const int cpos = cyc % 12;
+            wait = (phase == kStage && stage == 2 && cpos != 0) || (phase == kStartPass && cpos != 11);
+        }
+        ++cyc;
+        const bool active = live && !wait;
         n_all += leader ? 1ull : 0ull;
         n_useful += (active && leader) ? 1ull : 0ull;
         n_bin += active ? 1 : 0;
