@@ -129,11 +129,13 @@ EOB_HD double ipow(double x)
     }
 }
 
-// contribution m^2 |h_lm|^2 / (omega^2) of one (l, m); TP = (m x)/(1 - e^{-m x})
-// prod_{j<=l} (4k^2 + j^2).  rho_lm by fma Horner, rho^l by squaring, the
-// constant m^2 |h^N_lm|^2 / (l!)^2 from the table, S^2 once per parity.
+// contribution m^2 |h_lm|^2 / (omega^2) of one (l, m) without the factors
+// its m and parity share: P = prod_{j<=l} (4k^2 + j^2) times the constant
+// m^2 |h^N_lm|^2 / (l!)^2 from the table, rho^2l and v_phi^(2 (l + eps));
+// flux_m multiplies the even- and odd-parity sums by S_e^2 and S_o^2 and the
+// whole by (m x)/(1 - e^{-m x}).  rho_lm by fma Horner, rho^l by squaring.
 template <int l, int m, class Tab>
-EOB_HD double flux_term(const Tab &t, const FluxShared &s, double TP, const double *vp2)
+EOB_HD double flux_term(const Tab &t, const FluxShared &s, double P, const double *vp2)
 {
     constexpr int i = (l - 2) * (l + 1) / 2 + (m - 1);
     constexpr int eps = (l + m) % 2;
@@ -162,19 +164,25 @@ EOB_HD double flux_term(const Tab &t, const FluxShared &s, double TP, const doub
     } else if (m % 2 == 1) {
         rpl = (t.c_equal() != 0.0) ? 0.0 : rpl;
     }
-    const double S2 = eps ? s.S2o : s.S2e;
-    return t.c_gmul(i, l, m) * TP * S2 * (rpl * rpl) * vp2[l + eps];
+    return t.c_gmul(i, l, m) * P * (rpl * rpl) * vp2[l + eps];
 }
 
-// Accumulate all l for one m (products over j carried across l).
-template <int m, int l, class Tab>
-EOB_HD double flux_m_l(const Tab &t, const FluxShared &s, double Tpre, double P, double k2x4, const double *vp2)
+// Accumulate all l for one m (products over j carried across l) into the
+// even- and odd-parity sums; HE, HO: a term of that parity is already in.
+template <int m, int l, bool HE, bool HO, class Tab>
+EOB_HD void flux_m_l(const Tab &t, const FluxShared &s, double P, double k2x4, const double *vp2, double &se,
+                     double &so)
 {
     P *= k2x4 + (double)(l * l);
-    double here = 0.0;
-    if constexpr (l >= (m > 2 ? m : 2)) here = flux_term<l, m, Tab>(t, s, Tpre * P, vp2);
-    if constexpr (l < kLMax) return here + flux_m_l<m, l + 1, Tab>(t, s, Tpre, P, k2x4, vp2);
-    else return here;
+    constexpr bool use = (l >= (m > 2 ? m : 2));
+    constexpr bool even = ((l + m) % 2 == 0);
+    if constexpr (use) {
+        const double v = flux_term<l, m, Tab>(t, s, P, vp2);
+        if constexpr (even) se = HE ? se + v : v;
+        else so = HO ? so + v : v;
+    }
+    if constexpr (l < kLMax)
+        flux_m_l<m, l + 1, HE || (use && even), HO || (use && !even), Tab>(t, s, P, k2x4, vp2, se, so);
 }
 
 template <int m, class Tab>
@@ -183,7 +191,9 @@ EOB_HD double flux_m(const Tab &t, const FluxShared &s, double Em, double hw, co
     const double mx = m * s.x;
     const double Tpre = mx * eob_rcp(1.0 - Em);  // (4 pi k)/(1 - exp(-4 pi k)), k = m H omega
     const double km = m * hw;
-    return flux_m_l<m, 1, Tab>(t, s, Tpre, 1.0, 4.0 * km * km, vp2);
+    double se = 0.0, so = 0.0;
+    flux_m_l<m, 1, false, false, Tab>(t, s, 1.0, 4.0 * km * km, vp2, se, so);
+    return Tpre * fma(s.S2e, se, s.S2o * so);
 }
 
 // Radiation-reaction flux (before the division by nu of RR_force).
