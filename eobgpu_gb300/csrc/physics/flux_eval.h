@@ -129,6 +129,52 @@ EOB_HD double ipow(double x)
     }
 }
 
+// prod_{j=1..l} (x + j^2) = sum_i kTprod[l][i] x^i (exact integers)
+#define EOB_TPROD_INIT                                                                                       \
+    {{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {4.0, 5.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
+     {36.0, 49.0, 14.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                       \
+     {576.0, 820.0, 273.0, 30.0, 1.0, 0.0, 0.0, 0.0, 0.0},                                                   \
+     {14400.0, 21076.0, 7645.0, 1023.0, 55.0, 1.0, 0.0, 0.0, 0.0},                                           \
+     {518400.0, 773136.0, 296296.0, 44473.0, 3003.0, 91.0, 1.0, 0.0, 0.0},                                   \
+     {25401600.0, 38402064.0, 15291640.0, 2475473.0, 191620.0, 7462.0, 140.0, 1.0, 0.0},                    \
+     {1625702400.0, 2483133696.0, 1017067024.0, 173721912.0, 14739153.0, 669188.0, 16422.0, 204.0, 1.0}}
+static constexpr double kTprodH[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
+#ifdef __CUDACC__
+__device__ const double kTprodD[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
+#endif
+
+EOB_HD const double *tprod_row(int l)
+{
+#ifdef __CUDA_ARCH__
+    return kTprodD[l];
+#else
+    return kTprodH[l];
+#endif
+}
+
+// prod_{j=1..L} (x + j^2) for a compile-time L by Horner on the table's exact
+// integer coefficients (leading coefficient 1): L FP64 instructions
+template <int L, int Q>
+struct TprodHorner {
+    static EOB_HD double eval(double x, double p)
+    {
+        constexpr double c = kTprodH[L][Q];
+        return TprodHorner<L, Q - 1>::eval(x, fma(p, x, c));
+    }
+};
+template <int L>
+struct TprodHorner<L, -1> {
+    static EOB_HD double eval(double, double p) { return p; }
+};
+template <int L>
+EOB_HD double tprod_poly(double x)
+{
+    constexpr double c = kTprodH[L][L - 1];
+    return TprodHorner<L, L - 2>::eval(x, x + c);
+}
+
 // contribution m^2 |h_lm|^2 / (omega^2) of one (l, m) without the factors
 // its m and parity share: P = prod_{j<=l} (4k^2 + j^2) times the constant
 // m^2 |h^N_lm|^2 / (l!)^2 from the table, rho^2l and v_phi^(2 (l + eps));
@@ -167,22 +213,20 @@ EOB_HD double flux_term(const Tab &t, const FluxShared &s, double P, const doubl
     return t.c_gmul(i, l, m) * P * (rpl * rpl) * vp2[l + eps];
 }
 
-// Accumulate all l for one m (products over j carried across l) into the
-// even- and odd-parity sums; HE, HO: a term of that parity is already in.
+// Accumulate l = lmin..8 for one m into the even- and odd-parity sums; on
+// entry P = prod_{j<=l} (4 k^2 + j^2), carried across l; HE, HO: a term of
+// that parity is already in.
 template <int m, int l, bool HE, bool HO, class Tab>
 EOB_HD void flux_m_l(const Tab &t, const FluxShared &s, double P, double k2x4, const double *vp2, double &se,
                      double &so)
 {
-    P *= k2x4 + (double)(l * l);
-    constexpr bool use = (l >= (m > 2 ? m : 2));
     constexpr bool even = ((l + m) % 2 == 0);
-    if constexpr (use) {
-        const double v = flux_term<l, m, Tab>(t, s, P, vp2);
-        if constexpr (even) se = HE ? se + v : v;
-        else so = HO ? so + v : v;
-    }
+    const double v = flux_term<l, m, Tab>(t, s, P, vp2);
+    if constexpr (even) se = HE ? se + v : v;
+    else so = HO ? so + v : v;
     if constexpr (l < kLMax)
-        flux_m_l<m, l + 1, HE || (use && even), HO || (use && !even), Tab>(t, s, P, k2x4, vp2, se, so);
+        flux_m_l<m, l + 1, HE || even, HO || !even, Tab>(t, s, P * (k2x4 + (double)((l + 1) * (l + 1))), k2x4, vp2,
+                                                          se, so);
 }
 
 template <int m, class Tab>
@@ -191,8 +235,10 @@ EOB_HD double flux_m(const Tab &t, const FluxShared &s, double Em, double hw, co
     const double mx = m * s.x;
     const double Tpre = mx * eob_rcp(1.0 - Em);  // (4 pi k)/(1 - exp(-4 pi k)), k = m H omega
     const double km = m * hw;
+    const double k2x4 = 4.0 * km * km;
+    constexpr int lmin = (m > 2) ? m : 2;
     double se = 0.0, so = 0.0;
-    flux_m_l<m, 1, false, false, Tab>(t, s, 1.0, 4.0 * km * km, vp2, se, so);
+    flux_m_l<m, lmin, false, false, Tab>(t, s, tprod_poly<lmin>(k2x4), k2x4, vp2, se, so);
     return Tpre * fma(s.S2e, se, s.S2o * so);
 }
 
@@ -361,30 +407,6 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
 // shuffles; the Gamma product prod_{j<=l} (4 k^2 + j^2) is a polynomial in
 // 4 k^2 from a table; powers of v_phi^2 are precomputed and selected.
 
-// prod_{j=1..l} (x + j^2) = sum_i kTprod[l][i] x^i (exact integers)
-#define EOB_TPROD_INIT                                                                                       \
-    {{1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
-     {1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
-     {4.0, 5.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                          \
-     {36.0, 49.0, 14.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0},                                                       \
-     {576.0, 820.0, 273.0, 30.0, 1.0, 0.0, 0.0, 0.0, 0.0},                                                   \
-     {14400.0, 21076.0, 7645.0, 1023.0, 55.0, 1.0, 0.0, 0.0, 0.0},                                           \
-     {518400.0, 773136.0, 296296.0, 44473.0, 3003.0, 91.0, 1.0, 0.0, 0.0},                                   \
-     {25401600.0, 38402064.0, 15291640.0, 2475473.0, 191620.0, 7462.0, 140.0, 1.0, 0.0},                    \
-     {1625702400.0, 2483133696.0, 1017067024.0, 173721912.0, 14739153.0, 669188.0, 16422.0, 204.0, 1.0}}
-static constexpr double kTprodH[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
-#ifdef __CUDACC__
-__device__ const double kTprodD[kLMax + 1][kLMax + 1] = EOB_TPROD_INIT;
-#endif
-
-EOB_HD const double *tprod_row(int l)
-{
-#ifdef __CUDA_ARCH__
-    return kTprodD[l];
-#else
-    return kTprodH[l];
-#endif
-}
 
 // per-call pieces shared by every multipole of one lane group
 struct FluxLane {

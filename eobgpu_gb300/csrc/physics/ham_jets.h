@@ -418,6 +418,22 @@ EOB_HD void ham_eval_jets(const HamJets &J, double r, double pr, double L, HamEv
 }
 
 #ifdef __CUDACC__
+// Lane groups evaluate the jets in rounds, the seven jets with log r or
+// sqrt(u) parts first (AK0, Dbpm, q4, q6, q8, N0, N1), so that rounds past
+// them evaluate the polynomial part alone: with 8 lanes per binary the second
+// round costs 12 FP64 instructions instead of jet_eval's 40.
+constexpr int kJetsWithParts = 7;
+__device__ const signed char kJetOrderD[kNumJets] = {J_AK0, J_DB, J_Q4, J_Q6, J_Q8, J_N0, J_N1, J_AKA,
+                                                     J_FA,  J_AS, J_DC, J_G,  J_BX, J_BNN, J_N2, J_N3};
+
+// position of jet j in that order
+EOB_HD constexpr int jet_pos(int j)
+{
+    return j == J_AK0 ? 0 : j == J_DB ? 1 : j == J_Q4 ? 2 : j == J_Q6 ? 3 : j == J_Q8 ? 4 : j == J_N0 ? 5
+         : j == J_N1 ? 6 : j == J_AKA ? 7 : j == J_FA ? 8 : j == J_AS ? 9 : j == J_DC ? 10 : j == J_G ? 11
+         : j == J_BX ? 12 : j == J_BNN ? 13 : j == J_N2 ? 14 : 15;
+}
+
 // G lanes (2 .. 32, power of two) of one binary: jets split over the lanes,
 // full state on even lanes and p_r = 0 on odd lanes; every lane returns the
 // same result.  All 32 lanes of the warp must call it together.
@@ -431,16 +447,17 @@ __device__ __forceinline__ void ham_eval_group(const HamJets &J, double r, doubl
     double mv[R], md[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-        const int j = (q * G + sub) & (kNumJets - 1);
-        const Jet t = jet_eval(J, j, u, r, lr, su);
+        const int j = kJetOrderD[(q * G + sub) & (kNumJets - 1)];
+        const Jet t = (q * G < kJetsWithParts) ? jet_eval(J, j, u, r, lr, su) : jet_half(J, j, false, u, r, 1.0);
         mv[q] = t.v;
         md[q] = t.d;
     }
     Jet jt[kNumJets];
 #pragma unroll
     for (int j = 0; j < kNumJets; ++j) {
-        jt[j].v = __shfl_sync(0xffffffffu, mv[j / G], j % G, G);
-        jt[j].d = __shfl_sync(0xffffffffu, md[j / G], j % G, G);
+        const int p = jet_pos(j);
+        jt[j].v = __shfl_sync(0xffffffffu, mv[p / G], p % G, G);
+        jt[j].d = __shfl_sync(0xffffffffu, md[p / G], p % G, G);
     }
     const HamPart p = ham_combine(J, jt, u, (sub & 1) ? 0.0 : pr, L);
     out->H = __shfl_sync(0xffffffffu, p.H, 0, G);
