@@ -571,21 +571,24 @@ EOB_HD double flux_mode_vp_sq(int i, double vphi2)
     return r;
 }
 
+// LD: an upper bound on l of the multipoles evaluated together (the table's
+// coefficients above l are zero)
+template <int LD = kLMax>
 EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
 {
     const int l = lm_packed(i) >> 4;
     // prod_{j<=l} (4 k^2 + j^2)
     const double *c = tprod_row(l);
-    double P = c[kLMax];
+    double P = c[LD];
 #pragma unroll
-    for (int q = kLMax - 1; q >= 0; --q) P = fma(P, k4, c[q]);
+    for (int q = LD - 1; q >= 0; --q) P = fma(P, k4, c[q]);
     return t.gmul[i] * T * P;
 }
 
-template <int KMAX>
+template <int KMAX, int LD = kLMax>
 EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
 {
-    return flux_mode_b(t, i, T, k4) * flux_mode_a<KMAX>(t, i, f);
+    return flux_mode_b<LD>(t, i, T, k4) * flux_mode_a<KMAX>(t, i, f);
 }
 
 // Sequential use of the lane-group pieces (host tests)
@@ -640,6 +643,17 @@ __device__ __forceinline__ double flux_rounds(const FluxTable &t, const FluxShar
     }
 }
 
+// l of the multipoles at the sorted positions of kFluxOrder, and the largest
+// l among positions [first, first + n)
+constexpr int kFluxLSorted[kNumLM] = {2, 2, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 5, 6, 6, 6, 6,
+                                      6, 6, 7, 7, 7, 7, 7, 7, 7, 8, 8, 8, 8, 8, 8, 8, 8};
+EOB_HD constexpr int flux_lmax(int first, int n)
+{
+    int m = 0;
+    for (int p = first; p < first + n && p < kNumLM; ++p) m = kFluxLSorted[p] > m ? kFluxLSorted[p] : m;
+    return m;
+}
+
 template <int G, int R>
 __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const FluxLane &f, double Tm, double k4m,
                                                    int sub)
@@ -649,13 +663,14 @@ __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const Flu
         return 0.0;
     } else {
         constexpr int KM = kFluxDegSorted[first];
+        constexpr int LD = flux_lmax(first, G);
         const int pos = first + sub;
         const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
         const int m = lm_packed(i) & 15;
         // the m factors live on lanes m-1 of the group
         const double T = __shfl_sync(0xffffffffu, Tm, m - 1, G);
         const double k4 = __shfl_sync(0xffffffffu, k4m, m - 1, G);
-        double here = flux_mode_lane<KM>(t, i, f, T, k4);
+        double here = flux_mode_lane<KM, LD>(t, i, f, T, k4);
         if (pos >= kNumLM) here = 0.0;
         return here + flux_rounds_lane<G, R + 1>(t, f, Tm, k4m, sub);
     }
