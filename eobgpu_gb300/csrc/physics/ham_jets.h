@@ -43,6 +43,12 @@ enum JetId : int {
 struct HamJets {
     double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
     double n4, apsq, nu, M;
+    // The log r and sqrt(u) polynomials have one or two adjacent terms per
+    // jet: L = u^k (a + b u) with k = lk (3..5) and lc = {a, b, k a, (k+1) b};
+    // S = s u^k with k = sk (2..6) and sc = {s, k s} (zero where a jet has no
+    // such part), evaluated from powers of u instead of degree-6 Horner sums.
+    double lc[kNumJets][4], sc[kNumJets][2];
+    signed char lk[kNumJets], sk[kNumJets];
 };
 
 EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
@@ -93,30 +99,86 @@ EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
     J->l[J_N1][3] = h.ncl[1][3];
     for (int k = 0; k <= 2; ++k) J->c[J_N2][k] = h.nc[2][k];
     for (int k = 0; k <= 1; ++k) J->c[J_N3][k] = h.nc[3][k];
+    // sparse forms: the lowest log term (the tables above set at most two
+    // adjacent ones, at k = 3..6) and the single sqrt(u) term (k = 2..6)
+    for (int j = 0; j < kNumJets; ++j) {
+        int kl = 3, ks = 2;
+        for (int k = kJetTerms - 1; k >= 2; --k) {
+            if (J->l[j][k] != 0.0) kl = k;
+            if (J->s[j][k] != 0.0) ks = k;
+        }
+        if (kl > 5) kl = 5;
+        const double a = J->l[j][kl], b = J->l[j][kl + 1];
+        J->lk[j] = (signed char)kl;
+        J->lc[j][0] = a;
+        J->lc[j][1] = b;
+        J->lc[j][2] = kl * a;
+        J->lc[j][3] = (kl + 1) * b;
+        J->sk[j] = (signed char)ks;
+        J->sc[j][0] = J->s[j][ks];
+        J->sc[j][1] = ks * J->s[j][ks];
+    }
     J->n4 = h.nc[4][0];
     J->apsq = h.apsq;
     J->nu = h.nu;
     J->M = h.M;
 }
 
-// value and d/du of jet j at u (r = 1/u, lr = log r, su = sqrt(u))
+// powers of u for the sparse log r and sqrt(u) polynomials
+struct UPow {
+    double u, u2, u3, u4, u5;
+};
+
+EOB_HD UPow upow(double u)
+{
+    UPow p;
+    p.u = u;
+    p.u2 = u * u;
+    p.u3 = p.u2 * u;
+    p.u4 = p.u2 * p.u2;
+    p.u5 = p.u4 * u;
+    return p;
+}
+
+// u^k, k = 1..5 (selects, no arithmetic)
+EOB_HD double upow_sel(const UPow &p, int k)
+{
+    return k == 1 ? p.u : k == 2 ? p.u2 : k == 3 ? p.u3 : k == 4 ? p.u4 : p.u5;
+}
+
+// the log(r) polynomial itself (L, dL/du), without the factor log r: four
+// warps evaluate it beside log r and join the pieces afterwards (jet_join_s)
+EOB_HD Jet jet_poly_l(const HamJets &J, int j, const UPow &p)
+{
+    const double *c = J.lc[j];
+    const double pk = upow_sel(p, J.lk[j] - 1);  // u^(k-1)
+    return {(pk * p.u) * fma(c[1], p.u, c[0]), pk * fma(c[3], p.u, c[2])};
+}
+
+// the sqrt(u) polynomial itself (S, dS/du), without the factor sqrt(u)
+EOB_HD Jet jet_poly_s(const HamJets &J, int j, const UPow &p)
+{
+    const double pk = upow_sel(p, J.sk[j] - 1);  // u^(k-1)
+    return {(pk * p.u) * J.sc[j][0], pk * J.sc[j][1]};
+}
+
+// value and d/du of jet j at u (r = 1/u, lr = log r, su = sqrt(u)): the
+// polynomial part by Horner, the log r and sqrt(u) parts from their sparse
+// forms; d(log r)/du = -r, d(sqrt u)/du = sqrt(u) r / 2
 EOB_HD Jet jet_eval(const HamJets &J, int j, double u, double r, double lr, double su)
 {
-    const double *c = J.c[j], *l = J.l[j], *s = J.s[j];
-    double cv = c[6], cd = 0.0, lv = l[6], ld = 0.0, sv = s[6], sd = 0.0;
+    const double *c = J.c[j];
+    double cv = c[6], cd = 0.0;
 #pragma unroll
     for (int k = 5; k >= 0; --k) {
         cd = fma(cd, u, cv);
         cv = fma(cv, u, c[k]);
-        ld = fma(ld, u, lv);
-        lv = fma(lv, u, l[k]);
-        sd = fma(sd, u, sv);
-        sv = fma(sv, u, s[k]);
     }
-    // d(log r)/du = -r, d(sqrt u)/du = sqrt(u) r / 2
+    const UPow p = upow(u);
+    const Jet l = jet_poly_l(J, j, p), sq = jet_poly_s(J, j, p);
     Jet out;
-    out.v = fma(su, sv, fma(lr, lv, cv));
-    out.d = fma(su, fma(0.5 * r, sv, sd), fma(lr, ld, fma(-r, lv, cd)));
+    out.v = fma(su, sq.v, fma(lr, l.v, cv));
+    out.d = fma(su, fma(0.5 * r, sq.v, sq.d), fma(lr, l.d, fma(-r, l.v, cd)));
     return out;
 }
 
@@ -350,44 +412,11 @@ EOB_HD Jet jet_half(const HamJets &J, int j, bool sq, double u, double r, double
 
 EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
 {
-    const double *l = J.l[j];
-    double lv = l[6], ld = 0.0;
-#pragma unroll
-    for (int k = 5; k >= 0; --k) {
-        ld = fma(ld, u, lv);
-        lv = fma(lv, u, l[k]);
-    }
+    const Jet l = jet_poly_l(J, j, upow(u));
     Jet out;
-    out.v = lr * lv;
-    out.d = fma(lr, ld, -r * lv);
+    out.v = lr * l.v;
+    out.d = fma(lr, l.d, -r * l.v);
     return out;
-}
-
-// the log(r) polynomial itself (L, dL/du), without the factor log r: four
-// warps evaluate it beside log r and join the pieces afterwards (jet_join_s)
-EOB_HD Jet jet_poly_l(const HamJets &J, int j, double u)
-{
-    const double *l = J.l[j];
-    double lv = l[6], ld = 0.0;
-#pragma unroll
-    for (int k = 5; k >= 0; --k) {
-        ld = fma(ld, u, lv);
-        lv = fma(lv, u, l[k]);
-    }
-    return {lv, ld};
-}
-
-// the sqrt(u) polynomial itself (S, dS/du), without the factor sqrt(u)
-EOB_HD Jet jet_poly_s(const HamJets &J, int j, double u)
-{
-    const double *c = J.s[j];
-    double sv = c[6], sd = 0.0;
-#pragma unroll
-    for (int k = 5; k >= 0; --k) {
-        sd = fma(sd, u, sv);
-        sv = fma(sv, u, c[k]);
-    }
-    return {sv, sd};
 }
 
 // a jet from its polynomial part p, the sqrt(u) and log polynomials s and l,

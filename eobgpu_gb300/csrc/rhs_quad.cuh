@@ -64,13 +64,13 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         x.jet[1][0][lane] = p.v;
         x.jet[1][1][lane] = p.d;
     } else if (q == 2) {
-        const Jet p = jet_poly_s(J, j, u);
+        const Jet p = jet_poly_s(J, j, upow(u));
         x.jet[2][0][lane] = p.v;
         x.jet[2][1][lane] = p.d;
     } else {
         // sqrt(u) = 1/sqrt(r), beside the division u = 1/r
         const double su = eob_rsqrt(r);
-        const Jet p = jet_poly_l(J, j, u);
+        const Jet p = jet_poly_l(J, j, upow(u));
         x.jet[0][0][lane] = p.v;
         x.jet[0][1][lane] = p.d;
         if (lane == 0) {

@@ -88,8 +88,8 @@ void phys_ham_quad(const double *st, const double *add, int n, double *out)
         const double u = 1.0 / r, lr = eob::eob_log(r), su = eob::eob_rsqrt(r);
         eob::Jet jt[eob::kNumJets];
         for (int j = 0; j < eob::kNumJets; ++j)
-            jt[j] = eob::jet_join_s(eob::jet_half(J, j, false, u, r, 1.0), eob::jet_poly_s(J, j, u),
-                                    eob::jet_poly_l(J, j, u), su, 0.5 * r * su, lr, r);
+            jt[j] = eob::jet_join_s(eob::jet_half(J, j, false, u, r, 1.0), eob::jet_poly_s(J, j, eob::upow(u)),
+                                    eob::jet_poly_l(J, j, eob::upow(u)), su, 0.5 * r * su, lr, r);
         const double idc = 1.0 / jt[eob::J_DC].v;
         double res[2][5];
         for (int z = 0; z < 2; ++z) {
