@@ -4,7 +4,8 @@
 // binaries whose sequential chains set a batch's time:
 //
 //   stage           warp 0              warp 1              warp 2              warp 3
-//   jets            log r               polynomial parts    sqrt(u) polynomials log polynomials, sqrt(u)
+//   jets            log r               polynomial parts    sqrt(u) polynomials log polynomials
+//                                                           and sqrt(u)
 //   combination a   1/Dc, A(u)          1/Dc, c(u),         B_np, q, W - L^2 c  N(u, p_r^2)
 //                                       q part of dW/dp_r
 //   combination b   even part sqrt(AW)  odd part            --                  y_2/y_3, 1/(8 pi nu)
@@ -27,7 +28,7 @@ namespace eob {
 struct QuadXchg {
     double jet[3][2][32];  // jets: [log polynomial, polynomial, sqrt part][v, d][lane]
     double lr;             // warp 0: log r
-    double su[2];          // warp 3: sqrt(u) = 1/sqrt(r), r sqrt(u) / 2
+    double su[2];          // warp 2: sqrt(u) = 1/sqrt(r), r sqrt(u) / 2
     double pa[2][32];      // warp 0: A, dA/du
     double pc[2][32];      // warp 1: c, dc/du
     double pw[3][32];      // warp 2: W - L^2 c and its u-derivative, the B_np part of dW/dp_r
@@ -64,19 +65,19 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         x.jet[1][0][lane] = p.v;
         x.jet[1][1][lane] = p.d;
     } else if (q == 2) {
+        // sqrt(u) = 1/sqrt(r), beside the division u = 1/r
+        const double su = eob_rsqrt(r);
         const Jet p = jet_poly_s(J, j, upow(u));
         x.jet[2][0][lane] = p.v;
         x.jet[2][1][lane] = p.d;
-    } else {
-        // sqrt(u) = 1/sqrt(r), beside the division u = 1/r
-        const double su = eob_rsqrt(r);
-        const Jet p = jet_poly_l(J, j, upow(u));
-        x.jet[0][0][lane] = p.v;
-        x.jet[0][1][lane] = p.d;
         if (lane == 0) {
             x.su[0] = su;
             x.su[1] = 0.5 * r * su;
         }
+    } else {
+        const Jet p = jet_poly_l(J, j, upow(u));
+        x.jet[0][0][lane] = p.v;
+        x.jet[0][1][lane] = p.d;
     }
     pair_sync(ps);  // 1: jets
     // poly + sqrt(u) poly + log r * log poly, the same expression on every
