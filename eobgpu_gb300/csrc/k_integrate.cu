@@ -713,7 +713,8 @@ cudaError_t launch_g(const IntArgs &a, int bs, int grid, cudaStream_t s)
     return cudaGetLastError();
 }
 
-// Lanes per binary: a power of two in [1, 64] (64: a warp pair).  One lane
+// Lanes per binary chosen from the batch size: a power of two in [1, 64]
+// (64: a warp pair, with a head of four-warp groups; 128 only on request).  One lane
 // per binary is the most efficient use of the FP64 pipe; more lanes per
 // binary shorten each binary's critical path when the batch cannot fill the
 // device.
