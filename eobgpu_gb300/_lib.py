@@ -51,9 +51,8 @@ _SIGS = {
                                  _P, _P, _P]),
     "eob_workspace_counters": (c_int, [_P, c_int, c_int, c_int, c_int, _P, _P]),
     "eob_fp64_probe": (c_int, [_P, c_int, c_int, c_int, _P]),
-    "eob_component_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
-    "eob_pair_probe": (c_int, [_P, c_int, c_int, _P, c_int, c_int, _P]),
     "eob_math_probe": (c_int, [_P, c_int, _P, _P]),
+    "eob_sync_expiry_hook": (c_int, [c_int, c_int, ctypes.c_uint, c_int, c_int, c_ll, _P, c_int, _P]),
     "eob_noalloc_scratch_bytes": (c_size_t, []),
     "eob_waveform_lnl_noalloc": (c_int, [_P, c_int, _P, _P, c_int, c_double, _P, c_int, c_double,
                                          ctypes.POINTER(EobOptions), _P, _P, _P]),

@@ -23,9 +23,6 @@ constexpr size_t kNaBytes = eob::ws_layout(kNaBatch, kNaSteps, kNaModes, kNaSamp
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
-constexpr int kMaxDevices = 64;
-void *g_noalloc_addr[kMaxDevices] = {nullptr};
-
 }  // namespace
 
 extern "C" size_t eob_noalloc_scratch_bytes(void) { return kNaBytes; }
@@ -35,18 +32,17 @@ extern "C" int eob_waveform_lnl_noalloc(const double *params, int B, const int *
                                         int *status, cudaStream_t stream)
 {
     if (B < 1 || B > kNaBatch || K < 1 || K > kNaModes || N < 1 || N > kNaSamples) return EOB_E_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return EOB_E_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return EOB_E_ARG;
-    if (!g_noalloc_addr[dev]) {
-        // first call on this device: the device address of the scratch array
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return EOB_E_CUDA;
-        g_noalloc_addr[dev] = p;
-    }
+    // The array's device address on the current device, looked up on every
+    // call: it is not a stream operation and costs far less than the launch,
+    // and a cached value would go stale if the context were reset (the
+    // module is then loaded again, possibly elsewhere).  The first lookup on a
+    // device loads the library's device code there, so that first call should
+    // come before any stream capture.
+    void *scratch = nullptr;
+    if (cudaGetSymbolAddress(&scratch, g_noalloc_scratch) != cudaSuccess || !scratch) return EOB_E_CUDA;
     // trajectory capacity is bounded by kNaSteps rows per binary
     eob_options o;
     if (opt) o = *opt; else eob_options_default(&o);
-    return eob_waveform_lnl(g_noalloc_addr[dev], kNaBytes, kNaBatch, kNaSteps, kNaModes, kNaSamples, params, nullptr,
-                            B, ells, mms, K, dt, data, N, amp, &o, lnl, status, stream);
+    return eob_waveform_lnl(scratch, kNaBytes, kNaBatch, kNaSteps, kNaModes, kNaSamples, params, nullptr, B, ells,
+                            mms, K, dt, data, N, amp, &o, lnl, status, stream);
 }

@@ -63,8 +63,10 @@ __device__ __forceinline__ unsigned long long global_ns()
 
 // Both warps of the pair arrive (all 64 lanes: each lane's shared and global
 // writes before the barrier are released to the other warp) and wait, with a
-// time limit, for the phase to complete.
-__device__ __forceinline__ void pair_sync(PairSync &ps)
+// time limit of limit_ns, for the phase to complete.  A warp whose wait runs
+// out marks itself failed (ps.ok = false) and skips every later barrier, so a
+// group in which one warp stopped arriving ends after one limit per warp.
+__device__ __forceinline__ void pair_sync_limit(PairSync &ps, unsigned long long limit_ns)
 {
     if (!ps.ok) return;
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(ps.bar) : "memory");
@@ -80,38 +82,14 @@ __device__ __forceinline__ void pair_sync(PairSync &ps)
             : "memory");
         if (done) break;
         if (i == 0) t0 = global_ns();
-        else if (global_ns() - t0 > kPairTimeoutNs || i >= kPairMaxPolls) break;
+        else if (global_ns() - t0 > limit_ns || i >= kPairMaxPolls) break;
     }
     ps.parity ^= 1u;
     if (!__all_sync(0xffffffffu, done)) ps.ok = false;
 }
 
-// The same barrier polled with the non-suspending test (a warp that waits
-// spins on its own sub-partition, where it is the only warp).
-__device__ __forceinline__ void pair_sync_spin(PairSync &ps)
-{
-    if (!ps.ok) return;
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(ps.bar) : "memory");
-    unsigned done = 0;
-    unsigned long long t0 = 0;
-    for (int i = 0;; ++i) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(ps.bar), "r"(ps.parity)
-            : "memory");
-        if (done) break;
-        if ((i & 255) == 0) {
-            if (i == 0) t0 = global_ns();
-            else if (global_ns() - t0 > kPairTimeoutNs) break;
-        }
-        if (i >= kPairMaxPolls) break;
-    }
-    ps.parity ^= 1u;
-    if (!__all_sync(0xffffffffu, done)) ps.ok = false;
-}
+// The integrator's barrier: the fixed limit kPairTimeoutNs.
+__device__ __forceinline__ void pair_sync(PairSync &ps) { pair_sync_limit(ps, kPairTimeoutNs); }
 
 // Set-up by the block's first thread, before any group barrier is used:
 // ngroups barriers of `arrivals` threads each (64 for a pair, 128 for four warps).

@@ -107,12 +107,13 @@ int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int
  * memory pool, a plugin host without allocator access, or a process that must
  * not call cudaMalloc while other work is in flight passes only its inputs
  * and outputs; the scratch is a fixed __device__ array of
- * eob_noalloc_scratch_bytes() bytes (about 12 MB) that every GPU loading the
- * library keeps until exit.  Limits: B <= 16 binaries, K = 1 mode,
+ * eob_noalloc_scratch_bytes() bytes (13 584 384 bytes, 13.6 MB) that every
+ * GPU loading the library keeps until exit.  Limits: B <= 16 binaries, K = 1 mode,
  * N <= 8192 samples, at most 4096 trajectory rows per binary (longer
  * trajectories end with EOB_ST_MAXSTEP); larger calls return EOB_E_ARG.
- * The first call on a device looks up the array's address and should come
- * before any stream capture.  All calls share the array and it keeps the
+ * Every call looks up the array's device address (cudaGetSymbolAddress, no
+ * allocation); the first call on a device also loads the library's device code
+ * there and should come before any stream capture.  All calls share the array and it keeps the
  * last call's contents: calls that overlap on the GPU (other streams or
  * threads) race and must be serialised by the caller.  Allocates nothing
  * (no cudaMalloc, cudaFree or allocating library call). */
@@ -156,29 +157,6 @@ int eob_workspace_views(void *workspace, int max_batch, int max_steps, int max_m
  * spent on binaries, [5] right-hand-side evaluations of all integrator lanes. */
 int eob_workspace_counters(void *workspace, int max_batch, int max_steps, int max_modes, int max_samples,
                            unsigned long long *out8, cudaStream_t stream);
-
-/* FP64 issue-rate probe: blocks x threads lanes each run iters x 8 independent
- * DFMA chains; out[blocks * threads] receives the chain sums.  Timing it gives
- * the device's FP64 peak used as the integrator's roofline. */
-int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream);
-/* Timing probe of one piece of the right-hand side on binary 0 of a prepared
- * workspace (bins from eob_workspace_views): which = 0 Hamiltonian and
- * gradient, 1 flux, 2 right-hand side, 3 right-hand side with 16 lanes per
- * binary, 4 flux with 16 lanes, 5 flux with 32 lanes, 6 Hamiltonian with 16
- * lanes, 7 Hamiltonian with 32 lanes, 8 right-hand side with 32 lanes. */
-int eob_component_probe(const void *bins, int which, int iters, double *out, int blocks, int threads,
-                        cudaStream_t stream);
-/* accuracy probe of the hot path's math (no reference counterpart): for each
- * of the n device doubles x, out[8 i + 0..7] = the hot path's reciprocal, the
- * device division 1/x, the hot path's x^(-1/3), the device rcbrt, the hot
- * path's log, the device log, the hot path's 1/sqrt(x), the step controller's
- * x^(-1/8); out: device, 8 n doubles */
-int eob_math_probe(const double *x, int n, double *out, cudaStream_t stream);
-/* warp-pair probes (no reference counterpart): which 0/1 = barrier round trip
- * (suspending / spinning wait, out int[blocks * 4]), 2 = the pair right-hand
- * side on binary 0 of `bins` (out double[blocks * 4]); threads a multiple of 64,
- * at most 256 */
-int eob_pair_probe(const void *bins, int which, int iters, void *out, int blocks, int threads, cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Reference-shaped entry points (src/eob.pyx, src/dopr853.pyx, src/tdinterp.pyx)
@@ -273,6 +251,34 @@ int eob_tdinterp(const long long *templateChannels_ptrs, const double *dataTime,
 int eob_all_in_one_likelihood(double *temp_sum, const double *hp_fd, const double *hc_fd, const double *data,
                               const double *psd, const double *Fplus, const double *Fcross, const double *time_shift,
                               double df, int num_bin_all, int nchannels, int data_length, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Measurement and test hooks.  Not part of the waveform path and without a
+ * counterpart in the reference: they exist so that the benchmark can measure
+ * its roofline denominator on the device it runs on and the tests can check
+ * the hot path's arithmetic and its bounded waits.
+ */
+
+/* FP64 issue-rate probe: blocks x threads lanes each run iters x 8 independent
+ * DFMA chains; out[blocks * threads] receives the chain sums.  Timing it gives
+ * the device's FP64 peak used as the integrator's roofline. */
+int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream);
+/* Accuracy probe of the hot path's math: for each of the n device doubles x,
+ * out[8 i + 0..7] = the hot path's reciprocal, the device division 1/x, the
+ * hot path's x^(-1/3), the device rcbrt, the hot path's log, the device log,
+ * the hot path's 1/sqrt(x), the step controller's x^(-1/8); out: device, 8 n
+ * doubles. */
+int eob_math_probe(const double *x, int n, double *out, cudaStream_t stream);
+/* The integrator's multi-warp group barrier with its wait limited to limit_ns
+ * (1e3..2e9; the integrator itself uses 2 s).  Blocks of 256 threads hold
+ * groups of group_warps (2 or 4) warps that pass `rounds` barriers (at most
+ * 4096), exchanging values through shared memory; in every group g < 32 with
+ * bit g of skip_mask set, warp skip_warp of the group leaves at round
+ * skip_round without arriving, so the group's other warps see their wait run
+ * out.  out: device int[blocks * 8 * 4], per warp (ok, barriers passed, values
+ * read back wrong, microseconds spent in the wait that ran out). */
+int eob_sync_expiry_hook(int group_warps, int rounds, unsigned skip_mask, int skip_round, int skip_warp,
+                         long long limit_ns, int *out, int blocks, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

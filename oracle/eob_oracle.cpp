@@ -703,59 +703,15 @@ void oracle_interpolate_td(const double *t, const double *y, double *c1, double 
     }
 }
 
+}  // extern "C"
+
 // ---------------------------------------------------------------------------
-// Whole path for one binary: IC, two-pass trajectory, multipoles, splines,
-// synthesis on the uniform grid and the white-noise likelihood.
-//
-// params: m1, m2 [Msun], chi1, chi2, f0 [Hz]
-// cfg: dt [s], N samples, modes (ls, ms, K), max_step, rtol, atol
-// data: d[N]; amp: template amplitude A (h_k = A Re sum_lm h_lm(t_k))
-// outputs (optional, may be null):
-//   ic[3] = (r0, pphi0, pr0); nsteps (trajectory rows); traj_t[max_step], traj_y[max_step][4]
-//   npts (waveform samples of this binary); h_out[N] complex (re, im interleaved, summed modes)
-// returns lnL; status codes in *status (0 ok, 1 bad trajectory)
-double oracle_lnl_one(const double *params, double dt, int N, const int *ls, const int *ms, int K, int max_step,
-                      double rtol, double atol, const double *data, double amp, double *ic, int *nsteps, double *traj_t,
-                      double *traj_y, int *npts, double *h_out, int *status)
+// Whole path for one binary: the pieces shared by the free-running and replayed runs.
+namespace {
+
+double post_trajectory(const Binary &b, const Dense &d, int L, double Mt, double dt, int N, const int *ls,
+                       const int *ms, int K, const double *data, double amp, int *npts, double *h_out)
 {
-    *status = 0;
-    const double m1 = params[0], m2 = params[1], chi1 = params[2], chi2 = params[3], f0 = params[4];
-    const double Mt = m1 + m2;
-    const double m1s = m1 / Mt, m2s = m2 / Mt;
-    const double omega0 = f0 * (Mt * eob::kMTSUN_SI * PI);
-    Binary b;
-    build_binary(b, m1s, m2s, chi1, chi2, omega0, 1);
-    // initial conditions (eob/seobnrv4phm.py:1966-2070)
-    const double r_guess = pow(omega0, -2.0 / 3.0);
-    double x[2] = {r_guess, sqrt(r_guess)};
-    root_find_cons(b.h, omega0, x, 1000, 1e-12);
-    const double r0 = x[0], pphi0 = x[1];
-    const double pr0 = root_find_diss(b.h, b.fc, b.a, r0, pphi0, -3e-2, 0.0, 1000, 1e-12, nullptr, 0);
-    if (ic) { ic[0] = r0; ic[1] = pphi0; ic[2] = pr0; }
-    // two-pass trajectory (eob/seobnrv4phm.py:2072-2136)
-    Dense d;
-    d.t.assign((size_t)max_step, 0.0);
-    d.y.assign((size_t)max_step * 4, 0.0);
-    d.y[0] = r0; d.y[1] = 0.0; d.y[2] = pr0; d.y[3] = pphi0;
-    const double tmax = 1e7 * 1e6;
-    int stopc = 0;
-    int S = integrate(b, d, 0, 0.01, false, max_step, tmax, rtol, atol, &stopc);
-    if (S < 2 || S >= max_step - 1) { *status = 1; }
-    const double t_stop = d.t[(S >= 1) ? S - 1 : 0];
-    const double t_des = t_stop - 10.0;
-    int idx = 0;
-    double best = fabs(d.t[0] - t_des);
-    for (int i = 1; i < max_step; ++i) {
-        const double dd = fabs(d.t[i] - t_des);
-        if (dd < best) { best = dd; idx = i; }
-    }
-    if (idx < 1) { *status = 1; idx = 1; }
-    for (int i = idx; i < max_step; ++i) { d.t[i] = 0.0; for (int q = 0; q < 4; ++q) d.y[4 * i + q] = 0.0; }
-    S = integrate(b, d, idx - 1, 0.05, true, max_step, tmax, rtol, atol, &stopc);
-    const int L = S + 1;
-    if (nsteps) *nsteps = L;
-    if (traj_t) for (int i = 0; i < L; ++i) traj_t[i] = d.t[i];
-    if (traj_y) for (int i = 0; i < 4 * L; ++i) traj_y[i] = d.y[i];
     // multipoles on the trajectory (eob/seobnrv4phm.py:2138-2221)
     const double nu = b.h.nu;
     std::vector<cplx> hl((size_t)K * L);
@@ -823,6 +779,109 @@ double oracle_lnl_one(const double *params, double dt, int N, const int *ls, con
             h_out[2 * k + 1] = (k < nuse) ? hsum[k].imag() : 0.0;
         }
     return -0.5 * lnl;
+}
+
+// the two adaptive passes of run_trajectory (eob/seobnrv4phm.py:2072-2136); returns the row count
+int free_trajectory(const Binary &b, Dense &d, int max_step, double rtol, double atol, double h_init, int *status)
+{
+    const double tmax = 1e7 * 1e6;
+    int stopc = 0;
+    int S = integrate(b, d, 0, h_init, false, max_step, tmax, rtol, atol, &stopc);
+    if (S < 2 || S >= max_step - 1) { *status = 1; }
+    const double t_stop = d.t[(S >= 1) ? S - 1 : 0];
+    const double t_des = t_stop - 10.0;
+    int idx = 0;
+    double best = fabs(d.t[0] - t_des);
+    for (int i = 1; i < max_step; ++i) {
+        const double dd = fabs(d.t[i] - t_des);
+        if (dd < best) { best = dd; idx = i; }
+    }
+    if (idx < 1) { *status = 1; idx = 1; }
+    for (int i = idx; i < max_step; ++i) { d.t[i] = 0.0; for (int q = 0; q < 4; ++q) d.y[4 * i + q] = 0.0; }
+    S = integrate(b, d, idx - 1, 0.05, true, max_step, tmax, rtol, atol, &stopc);
+    return S + 1;
+}
+
+// one always-accepted DOPR853 step per pair of consecutive given knots
+int replay_trajectory(const Binary &b, Dense &d, const double *knots, int L, double rtol, double atol, int *status)
+{
+    double k[11][4];
+    for (int i = 1; i < L; ++i) {
+        const double hstep = knots[i] - knots[i - 1];
+        if (!(hstep > 0.0)) { *status = 1; return i; }
+        double y[4], ynew[4];
+        for (int q = 0; q < 4; ++q) y[q] = d.y[4 * (i - 1) + q];
+        dopr_stages(b, y, hstep, k);
+        dopr_error(y, hstep, k, ynew, rtol, atol);
+        for (int q = 0; q < 4; ++q) d.y[4 * i + q] = ynew[q];
+        d.t[i] = knots[i];
+    }
+    return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Whole path for one binary: IC, trajectory, multipoles, splines, synthesis
+// on the uniform grid and the white-noise likelihood.
+//
+// params: m1, m2 [Msun], chi1, chi2, f0 [Hz]
+// cfg: dt [s], N samples, modes (ls, ms, K), max_step, rtol, atol
+// h_init: first step of the adaptive pass [M] (the reference's 0.01,
+//   eob/new_Dormand_horiz.py:527-531; another value samples the same
+//   trajectory on other knots)
+// replay_t (may be null): knot times [M] of a trajectory of replay_L rows,
+//   replay_t[0] = 0.  Instead of the two adaptive passes, the state is carried
+//   from row i - 1 to row i by one DOPR853 step of h = replay_t[i] -
+//   replay_t[i - 1], always accepted: the reference's integrator on a given
+//   sequence of accepted steps (every row of both passes is one accepted
+//   step from the row before it, src/DOPR853.cu:357-618), so that two
+//   implementations can be compared on the same knots.
+// data: d[N]; amp: template amplitude A (h_k = A Re sum_lm h_lm(t_k))
+// outputs (optional, may be null):
+//   ic[3] = (r0, pphi0, pr0); nsteps (trajectory rows); traj_t[max_step], traj_y[max_step][4]
+//   npts (waveform samples of this binary); h_out[N] complex (re, im interleaved, summed modes)
+// returns lnL; status codes in *status (0 ok, 1 bad trajectory)
+double oracle_lnl_ex(const double *params, double dt, int N, const int *ls, const int *ms, int K, int max_step,
+                     double rtol, double atol, double h_init, const double *replay_t, int replay_L,
+                     const double *data, double amp, double *ic, int *nsteps, double *traj_t, double *traj_y,
+                     int *npts, double *h_out, int *status)
+{
+    *status = 0;
+    const double m1 = params[0], m2 = params[1], chi1 = params[2], chi2 = params[3], f0 = params[4];
+    const double Mt = m1 + m2;
+    const double m1s = m1 / Mt, m2s = m2 / Mt;
+    const double omega0 = f0 * (Mt * eob::kMTSUN_SI * PI);
+    Binary b;
+    build_binary(b, m1s, m2s, chi1, chi2, omega0, 1);
+    // initial conditions (eob/seobnrv4phm.py:1966-2070)
+    const double r_guess = pow(omega0, -2.0 / 3.0);
+    double x[2] = {r_guess, sqrt(r_guess)};
+    root_find_cons(b.h, omega0, x, 1000, 1e-12);
+    const double r0 = x[0], pphi0 = x[1];
+    const double pr0 = root_find_diss(b.h, b.fc, b.a, r0, pphi0, -3e-2, 0.0, 1000, 1e-12, nullptr, 0);
+    if (ic) { ic[0] = r0; ic[1] = pphi0; ic[2] = pr0; }
+    if (replay_t && (replay_L < 2 || replay_L > max_step)) { *status = 1; return 0.0; }
+    Dense d;
+    d.t.assign((size_t)max_step, 0.0);
+    d.y.assign((size_t)max_step * 4, 0.0);
+    d.y[0] = r0; d.y[1] = 0.0; d.y[2] = pr0; d.y[3] = pphi0;
+    const int L = replay_t ? replay_trajectory(b, d, replay_t, replay_L, rtol, atol, status)
+                           : free_trajectory(b, d, max_step, rtol, atol, h_init, status);
+    if (nsteps) *nsteps = L;
+    if (traj_t) for (int i = 0; i < L; ++i) traj_t[i] = d.t[i];
+    if (traj_y) for (int i = 0; i < 4 * L; ++i) traj_y[i] = d.y[i];
+    if (L < 2) { *status = 1; return 0.0; }
+    return post_trajectory(b, d, L, Mt, dt, N, ls, ms, K, data, amp, npts, h_out);
+}
+
+double oracle_lnl_one(const double *params, double dt, int N, const int *ls, const int *ms, int K, int max_step,
+                      double rtol, double atol, const double *data, double amp, double *ic, int *nsteps, double *traj_t,
+                      double *traj_y, int *npts, double *h_out, int *status)
+{
+    return oracle_lnl_ex(params, dt, N, ls, ms, K, max_step, rtol, atol, 0.01, nullptr, 0, data, amp, ic, nsteps,
+                         traj_t, traj_y, npts, h_out, status);
 }
 
 // batch convenience: params[B][5]; lnl[B]; status[B]

@@ -54,6 +54,7 @@ class Oracle:
         lib.oracle_ctx_destroy.argtypes = [ctypes.c_void_p]
         lib.oracle_ctx_coeffs.argtypes = [ctypes.c_void_p, ctypes.c_int, P]
         lib.oracle_lnl_one.restype = ctypes.c_double
+        lib.oracle_lnl_ex.restype = ctypes.c_double
         self.nfac = lib.oracle_fac_ndouble()
 
     # --- Hamiltonian -------------------------------------------------------
@@ -90,7 +91,13 @@ class Oracle:
         return OracleContext(self, ctypes.c_void_p(p), len(m1))
 
     # --- whole path --------------------------------------------------------
-    def lnl_one(self, params, dt, N, modes, data, amp, max_step=20000, rtol=1e-12, atol=1e-12, want_detail=False):
+    def lnl_one(self, params, dt, N, modes, data, amp, max_step=20000, rtol=1e-12, atol=1e-12, want_detail=False,
+                h_init=0.01, replay_t=None):
+        """The whole path for one binary (IC, trajectory, modes, splines,
+        synthesis, lnL).  replay_t: knot times [M] of a trajectory computed
+        elsewhere (row 0 at t = 0); the oracle then carries its own state
+        from knot to knot with one accepted DOPR853 step each, instead of
+        choosing the steps itself.  h_init: first adaptive step [M]."""
         params = _f64(params)
         ls = np.ascontiguousarray([l for l, _ in modes], dtype=np.int32)
         ms = np.ascontiguousarray([m for _, m in modes], dtype=np.int32)
@@ -99,15 +106,21 @@ class Oracle:
         nsteps = ctypes.c_int(0)
         npts = ctypes.c_int(0)
         status = ctypes.c_int(0)
+        rt = None
+        if replay_t is not None:
+            rt = _f64(replay_t)
+            max_step = max(max_step, len(rt))
         tt = np.zeros(max_step) if want_detail else None
         yy = np.zeros((max_step, 4)) if want_detail else None
         hh = np.zeros(2 * N) if want_detail else None
-        lnl = self.lib.oracle_lnl_one(_dp(params), ctypes.c_double(dt), ctypes.c_int(N), _ip(ls), _ip(ms),
-                                      ctypes.c_int(len(ls)), ctypes.c_int(max_step), ctypes.c_double(rtol),
-                                      ctypes.c_double(atol), _dp(data), ctypes.c_double(amp), _dp(ic),
-                                      ctypes.byref(nsteps), _dp(tt) if tt is not None else None,
-                                      _dp(yy) if yy is not None else None, ctypes.byref(npts),
-                                      _dp(hh) if hh is not None else None, ctypes.byref(status))
+        lnl = self.lib.oracle_lnl_ex(_dp(params), ctypes.c_double(dt), ctypes.c_int(N), _ip(ls), _ip(ms),
+                                     ctypes.c_int(len(ls)), ctypes.c_int(max_step), ctypes.c_double(rtol),
+                                     ctypes.c_double(atol), ctypes.c_double(h_init),
+                                     _dp(rt) if rt is not None else None, ctypes.c_int(0 if rt is None else len(rt)),
+                                     _dp(data), ctypes.c_double(amp), _dp(ic),
+                                     ctypes.byref(nsteps), _dp(tt) if tt is not None else None,
+                                     _dp(yy) if yy is not None else None, ctypes.byref(npts),
+                                     _dp(hh) if hh is not None else None, ctypes.byref(status))
         out = {"lnl": lnl, "ic": ic, "nsteps": nsteps.value, "npts": npts.value, "status": status.value}
         if want_detail:
             L = nsteps.value

@@ -1,11 +1,30 @@
-"""Configuration 2 (ragged batching: M 20-200, q 1-8, chi up to 0.9, f0 10-20 Hz,
-N = 2^17) on the GPU against the oracle on a 64-binary sample, and the
-size-independent checks of the full batch (every binary finishes, lnL finite
-and bounded by the data)."""
+"""Configuration 2 (ragged batching: 1024 binaries, M 20-200, q 1-8, chi up to
+0.9, f0 10-20 Hz, dt = 1/2048 s, N = 2^17, FP64) on the GPU against the oracle
+on a 64-binary sample (every 16th binary), and the size-independent checks of
+the full batch.
+
+Two comparisons:
+* replay -- the oracle carried over the GPU's own accepted knots (one DOPR853
+  step per pair of rows, both passes): the FP64 tolerances hold for every
+  binary (relative lnL <= 1e-9, strain within 1e-8 of its peak, phase at the
+  peak within 1e-5 rad) and the trajectory rows agree to 1e-10 of scale;
+* free-running -- each side chooses its own steps.  The adaptive controller's
+  error estimate is a difference of slopes that cancels to ~1e-12 of the
+  state, so rounding-level differences re-sample the same trajectory on other
+  knots.  How far that moves the result is measured on the oracle alone
+  (tests/golden/config2_spread.npz: its first step moved by one ulp): up to
+  2.9e-8 in relative lnL and 1.2e-6 in peak amplitude, with 73 % of binaries
+  within 1e-9.  The GPU is held to four times that spread, and to the FP64
+  tolerance in its median.
+"""
+import os
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
@@ -26,11 +45,16 @@ def cfg2(oracle):
     npts = wl.npts()
     nsteps, _, _, trajs = wl.trajectories()
     idx = np.arange(0, len(params), 16)
-    t_sample = [trajs[b][0] for b in idx]
     hs, _ = wl.synth_strain(len(params), cfg.dt, cfg.n_samples)
     h_sample = hs[torch.tensor(idx, device="cuda")].cpu().numpy()
     del hs
-    return cfg, params, data, amp, lnl.cpu().numpy(), st.cpu().numpy(), npts, nsteps, (idx, h_sample, t_sample)
+    sample = {"idx": idx, "h": h_sample, "traj": [trajs[b] for b in idx]}
+    return cfg, params, data, amp, lnl.cpu().numpy(), st.cpu().numpy(), npts, nsteps, sample
+
+
+@pytest.fixture(scope="module")
+def spread():
+    return dict(np.load(os.path.join(HERE, "golden", "config2_spread.npz")))
 
 
 def test_config2_full_batch(cfg2):
@@ -48,36 +72,54 @@ def _peak_phase_amp(h):
     return k, np.angle(h[k]), a[k]
 
 
-def test_config2_sample_vs_oracle(cfg2, oracle):
-    """Every 16th binary against the oracle.  The adaptive controller's error
-    estimate is a difference of slopes that cancels to ~1e-12 of the state, so
-    rounding-level differences between two FP64 evaluations of the same RHS
-    move it by ~1e-4 relative.  Once the first steps stop growing at the
-    controller's maximum factor (row 6), every step size moves by ~1e-5
-    relative, and decisions with err close to 1 flip: any two FP64
-    implementations (this one at any lanes per binary, the oracle, the
-    reference's GPU and CPU builds) sample the same trajectory on different
-    knots.  Every binary is held to the waveform tolerance (phase at the
-    amplitude peak within 1e-5 rad, peak amplitude within 1e-5 relative, lnL
-    within 1e-6 relative); the median binary to the FP64 likelihood tolerance
-    (relative lnL 1e-9), and accept/reject flips (different row counts) are a
-    minority."""
-    cfg, params, data, amp, lnl, st, npts, nsteps, (idx, hg, tg) = cfg2
-    flips = 0
+def test_config2_replay_vs_oracle(cfg2, oracle):
+    """Every sampled binary on identical knots: the spec FP64
+    tolerances, per binary."""
+    cfg, params, data, amp, lnl, st, npts, nsteps, s = cfg2
+    worst = {"rows": 0.0, "strain": 0.0, "lnl": 0.0, "dphi": 0.0}
+    for j, b in enumerate(s["idx"]):
+        t, y = s["traj"][j]
+        r = oracle.lnl_one(params[b], cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, want_detail=True,
+                           replay_t=t)
+        assert r["status"] == 0 and r["nsteps"] == len(t)
+        assert r["npts"] == npts[b], (b, r["npts"], npts[b])
+        scale = np.max(np.abs(y), axis=0)
+        rows = float(np.max(np.abs(r["y"] - y) / scale))
+        ho, hg = r["h"], s["h"][j]
+        ko, po, ao = _peak_phase_amp(ho)
+        strain = float(np.max(np.abs(hg - ho)) / ao)
+        dphi = abs((np.angle(hg[ko]) - po + np.pi) % (2 * np.pi) - np.pi)
+        rel = abs(lnl[b] / r["lnl"] - 1)
+        for k, v in (("rows", rows), ("strain", strain), ("lnl", rel), ("dphi", dphi)):
+            worst[k] = max(worst[k], v)
+        assert rows <= 1e-10, (b, rows)
+        assert strain <= 1e-8, (b, strain)
+        assert dphi <= 1e-5, (b, dphi)
+        assert rel <= 1e-9, (b, lnl[b], r["lnl"], rel)
+    print("replay worst:", worst)
+
+
+def test_config2_free_running_vs_oracle(cfg2, oracle, spread):
+    """Each side on its own steps: within four times the oracle's own
+    one-ulp spread per binary, FP64 tolerance in the median."""
+    cfg, params, data, amp, lnl, st, npts, nsteps, s = cfg2
+    assert np.array_equal(spread["index"], s["idx"])
+    rel_bound = 4.0 * float(spread["rel_dlnl"].max())
+    amp_bound = 4.0 * float(spread["damp_peak"].max())
     rel = []
-    for j, b in enumerate(idx):
+    for j, b in enumerate(s["idx"]):
         r = oracle.lnl_one(params[b], cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, max_step=6000,
                            want_detail=True)
         assert r["status"] == 0
         ko, po, ao = _peak_phase_amp(r["h"])
-        kg, pg, ag = _peak_phase_amp(hg[j])
+        kg, pg, ag = _peak_phase_amp(s["h"][j])
         dphi = abs((pg - po + np.pi) % (2 * np.pi) - np.pi)
-        flips += int(r["npts"] != npts[b] or r["nsteps"] != nsteps[b])
         assert abs(r["npts"] - npts[b]) <= 1
         assert ko == kg, (b, ko, kg)
         assert dphi < 1e-5, (b, dphi)
-        assert abs(ag / ao - 1) < 1e-5, (b, ag, ao)
+        assert abs(ag / ao - 1) < amp_bound, (b, ag, ao, amp_bound)
         rel.append(abs(lnl[b] / r["lnl"] - 1))
-        assert rel[-1] < 1e-6, (b, lnl[b], r["lnl"])
+        assert rel[-1] < rel_bound, (b, lnl[b], r["lnl"], rel_bound)
+    rel = np.array(rel)
     assert np.median(rel) < 1e-9, sorted(rel)
-    assert flips <= len(idx) // 2, flips
+    assert np.mean(rel <= 1e-9) >= 0.5, np.mean(rel <= 1e-9)

@@ -1,5 +1,7 @@
 """The oracle against the reference's own outputs (tests/golden/, made by
 tests/golden/make_golden.py from the reference's host-compiled kernels)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -122,3 +124,48 @@ def test_config1_end_to_end(oracle, golden, b):
         h, hr = r["h"], c[f"h_{b}"]
         m = min(len(hr), len(h))
         assert np.max(np.abs(h[:m] - hr[:m])) < 1e-8 * np.abs(hr).max()
+
+
+@pytest.mark.parametrize("b", range(8))
+def test_config1_replay_on_reference_knots(oracle, golden, b):
+    """Replay mode: the oracle carried over the reference's own accepted knots
+    (one DOPR853 step per pair of rows) reproduces the reference's trajectory
+    rows and its likelihood -- the check that lets the CUDA path be compared
+    with the oracle on identical knots."""
+    c = golden["config1"]
+    L = int(c["nsteps"][b])
+    t = c["traj_t"][b, :L]
+    r = oracle.lnl_one(c["params"][b], float(c["dt"]), int(c["N"]), [(2, 2)], c["data"], float(c["amp"]),
+                       want_detail=True, replay_t=t)
+    assert r["status"] == 0 and r["nsteps"] == L and r["npts"] == c["npts"][b]
+    # rows within 1e-10 of each component's scale (measured: at most 4e-11,
+    # in p_r on the last rows of the plunge; up to 1.3e-11 at r > 3)
+    yr = c["traj_y"][b, :L]
+    scale = np.max(np.abs(yr), axis=0)
+    err = np.abs(r["y"] - yr) / scale
+    assert np.all(err.max(axis=0) <= 1e-10), err.max(axis=0)
+    assert np.all(err[yr[:, 0] > 3.0].max(axis=0) <= 3e-11), err[yr[:, 0] > 3.0].max(axis=0)
+    # lnL on identical knots: measured within 1e-13 (free-running: up to 4e-11)
+    assert abs(r["lnl"] / c["lnl"][b] - 1) < 1e-12, (r["lnl"], c["lnl"][b])
+    if f"h_{b}" in c:
+        h, hr = r["h"], c[f"h_{b}"]
+        m = min(len(hr), len(h))
+        assert np.max(np.abs(h[:m] - hr[:m])) < 1e-9 * np.abs(hr).max()
+
+
+def test_config2_spread_fixture_reproduces():
+    """tests/golden/config2_spread.npz (the oracle's own one-ulp spread on the
+    ragged-batching sample, which sets the GPU's free-running bounds) is what
+    tests/golden/make_spread.py computes: three binaries re-measured, the
+    largest spread among them."""
+    from golden import make_spread
+    from eobgpu_gb300 import workload
+    fx = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_spread.npz")))
+    cfg = workload.CONFIGS[2]
+    params = workload.draw_params(cfg)
+    data, amp = make_spread.data_vector(cfg)
+    for j in (int(np.argmax(fx["rel_dlnl"])), 0, len(fx["index"]) - 1):
+        b = int(fx["index"][j])
+        out = make_spread.one((params[b], cfg.dt, cfg.n_samples, data, amp))
+        assert out[0] == pytest.approx(fx["lnl"][j], rel=1e-12)
+        assert max(out[3], out[9]) == pytest.approx(fx["rel_dlnl"][j], rel=1e-3, abs=1e-15)
