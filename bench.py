@@ -6,12 +6,21 @@ f0 ~ U[10, 20] Hz, (2,2) mode, dt = 1/2048 s, N = 2^17 samples, white-noise
 data with one injection at SNR 30, FP64 throughout.  A step is one pass of the
 whole path (parameters -> lnL) over the batch.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference] [--config 1|2|3|5]
+    python bench.py [--gpus N] [--steps K] [--warmup W]
+                    [--impl native|reference|plain|refloop] [--config 1|2|3|4|5]
+
+The default line also carries, on one GPU, the plain FP64 GPU method on the
+same batch (`plain`, `vs_plain`) and the serving workload (`serving`: a
+2000-request Poisson trace of walker batches through the continuous-batching
+server in mixed precision, its capacity, request latency p50/p99 at 70 % load,
+and the plain method serving the same requests one at a time).
 
 Under torchrun (N > 1) every rank runs its own batch (replicas: the path has
 no exchange step); value = all binaries of all ranks / max-over-ranks time.
 `--impl reference` times the CPU restatement of the reference path (the
-oracle) on the host cores.  Prints one JSON line.
+oracle) on the host cores; `--impl plain` the plain FP64 GPU method alone;
+`--impl refloop` the reference's own launch structure (a host loop of
+per-stage launches) on the GPU.  Prints one JSON line.
 """
 from __future__ import annotations
 
@@ -32,25 +41,12 @@ from eobgpu_gb300 import workload  # noqa: E402
 
 METRIC = "waveform+lnL evals/s"
 # FP64 floating-point operations of one right-hand-side evaluation of the
-# integrator: hardware census (ncu DADD + DMUL + 2 DFMA thread instructions of
-# k_integrate divided by the lane-RHS count) -- profiles/k_integrate_fp64_census.md
-F_RHS = None  # filled from the census file at import time below
-
-CENSUS = os.path.join(ROOT, "profiles", "k_integrate_fp64_census.md")
-
-
-def _census_flops():
-    try:
-        with open(CENSUS) as f:
-            for line in f:
-                if line.startswith("F_RHS_FLOPS"):
-                    return float(line.split("=")[1].strip())
-    except OSError:
-        pass
-    return None
-
-
-F_RHS = _census_flops()
+# integrator, frozen: the hardware census of the one-lane kernel (ncu DADD +
+# DMUL + 2 DFMA thread instructions divided by the lane-RHS count,
+# profiles/k_integrate_fp64_census.md).  It stays fixed when later kernels
+# need fewer instructions per right-hand side, so that roofline fractions
+# compare across versions.
+F_RHS = 1533.0
 
 TRAFFIC = os.path.join(ROOT, "profiles", "k_integrate_traffic_config2.md")
 
@@ -166,19 +162,28 @@ def make_inputs(cfg, stream_seed, device, max_steps):
     return params, data, amp
 
 
+_POOL_DATA = None
+
+
+def _pool_init(data):
+    """Worker initialiser: the data vector is sent to each worker once."""
+    global _POOL_DATA
+    _POOL_DATA = data
+
+
 def _oracle_worker(args):
-    p, dt, N, modes, data, amp, max_step = args
+    p, dt, N, modes, amp, max_step = args
     from oracle.oracle import Oracle
     o = Oracle()
-    return o.lnl_one(p, dt, N, modes, data, amp, max_step=max_step)["lnl"]
+    return o.lnl_one(p, dt, N, modes, _POOL_DATA, amp, max_step=max_step)["lnl"]
 
 
 def cpu_time(params, cfg, data, amp, max_step, cores):
     """Wall time of the oracle (CPU restatement of the reference path) over params on `cores` processes."""
     import multiprocessing as mp
-    jobs = [(p, cfg.dt, cfg.n_samples, list(cfg.modes), data, amp, max_step) for p in params]
+    jobs = [(p, cfg.dt, cfg.n_samples, list(cfg.modes), amp, max_step) for p in params]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
+    with ctx.Pool(cores, initializer=_pool_init, initargs=(data,)) as pool:
         pool.map(_oracle_worker, jobs[:cores])  # start-up and first-call costs outside the timing
         t0 = time.perf_counter()
         out = pool.map(_oracle_worker, jobs, chunksize=1)
@@ -187,21 +192,28 @@ def cpu_time(params, cfg, data, amp, max_step, cores):
 
 
 def _oracle_detail_worker(args):
-    p, dt, N, modes, data, amp, max_step = args
+    """Free-running oracle, and the oracle replayed on the GPU's knots."""
+    p, dt, N, modes, amp, max_step, knots = args
     from oracle.oracle import Oracle
-    r = Oracle().lnl_one(p, dt, N, modes, data, amp, max_step=max_step, want_detail=True)
-    return r["lnl"], r["status"], r["h"], r["npts"]
+    o = Oracle()
+    r = o.lnl_one(p, dt, N, modes, _POOL_DATA, amp, max_step=max_step, want_detail=True)
+    rr = o.lnl_one(p, dt, N, modes, _POOL_DATA, amp, max_step=max_step, want_detail=True, replay_t=knots)
+    return (r["lnl"], r["status"], r["h"], r["npts"]), (rr["lnl"], rr["status"], rr["h"], rr["npts"], rr["y"])
 
 
 def accuracy_vs_oracle(params, cfg, data, amp, max_steps, precision, device, sample, cores):
     """Waveform and lnL error of the GPU path against the FP64 oracle on an
-    evenly spread sample of the batch (outside any timed region): phase and
-    relative amplitude at the oracle's amplitude peak, mismatch
-    1 - Re<a, c> / (|a| |c|) over the N samples, |dlnL| and |dlnL| / |lnL|.
-    Binaries whose template ends on another sample than the oracle's (the
-    two samplings of the trajectory stop on different sides of a sample
-    time; the last sample, at the merger, then carries h^2 ~ 25-50 of lnL)
-    are counted apart and their worst values reported separately."""
+    evenly spread sample of the batch (outside any timed region), two ways:
+
+    replay -- the oracle carried over the GPU's own accepted knots (one
+      DOPR853 step per pair of trajectory rows): identical sampling, so the
+      differences are the arithmetic's alone (rows, strain, lnL);
+    free-running -- each side chooses its own steps: phase and relative
+      amplitude at the oracle's amplitude peak, mismatch 1 - Re<a, c> /
+      (|a| |c|) over the N samples, |dlnL| and |dlnL| / |lnL|.  The adaptive
+      controller turns rounding-level differences into other knots; binaries
+      whose template ends on another sample than the oracle's (the last
+      sample, at the merger, carries h^2 ~ 25-50 of lnL) are counted apart."""
     import multiprocessing as mp
     import torch
     from eobgpu_gb300 import _lib
@@ -214,39 +226,57 @@ def accuracy_vs_oracle(params, cfg, data, amp, max_steps, precision, device, sam
     wl = WaveformLikelihood(len(P), max_steps, list(cfg.modes), N, device=device, options=o)
     Pd = torch.tensor(P, device=device)
     lnl, st = wl.run(Pd, torch.tensor(data, device=device), cfg.dt, amp)
-    hs, _ = wl.strain(Pd, cfg.dt, N)
+    hs, _ = wl.synth_strain(len(P), cfg.dt, N)
     lnl, st, hs = lnl.cpu().numpy(), st.cpu().numpy(), hs.cpu().numpy()
-    npts = wl.npts()
+    nsteps, npts, _, trajs = wl.trajectories()
     del wl, Pd
     torch.cuda.empty_cache()
-    jobs = [(p, cfg.dt, N, list(cfg.modes), data, amp, max_steps) for p in P]
-    with mp.get_context("spawn").Pool(cores) as pool:
+    jobs = [(p, cfg.dt, N, list(cfg.modes), amp, max_steps, trajs[b][0]) for b, p in enumerate(P)]
+    with mp.get_context("spawn").Pool(cores, initializer=_pool_init, initargs=(data,)) as pool:
         res = pool.map(_oracle_detail_worker, jobs, chunksize=1)
     m = {True: [], False: []}  # same end sample as the oracle: metrics
+    rep = []
     skipped = 0
-    for b, (ol, ost, a, onp) in enumerate(res):
-        if ost != 0 or st[b] != 0:
+    for b, ((ol, ost, a, onp), (rl, rst, ra, rnp, ry)) in enumerate(res):
+        if ost != 0 or st[b] != 0 or rst != 0:
             skipped += 1
             continue
         c = hs[b]
-        ov = np.real(np.vdot(a, c)) / np.sqrt(np.real(np.vdot(a, a)) * np.real(np.vdot(c, c)))
         k = int(np.argmax(np.abs(a)))
+        ov = np.real(np.vdot(a, c)) / np.sqrt(np.real(np.vdot(a, a)) * np.real(np.vdot(c, c)))
         m[int(npts[b]) == int(onp)].append((
             abs((np.angle(c[k]) - np.angle(a[k]) + np.pi) % (2 * np.pi) - np.pi), abs(abs(c[k]) / abs(a[k]) - 1),
             1 - ov, abs(lnl[b] - ol), abs(lnl[b] - ol) / abs(ol)))
+        y = trajs[b][1]
+        kr = int(np.argmax(np.abs(ra)))
+        rep.append((float(np.max(np.abs(y - ry) / np.max(np.abs(y), axis=0))),
+                    float(np.max(np.abs(c - ra)) / abs(ra[kr])),
+                    abs((np.angle(c[kr]) - np.angle(ra[kr]) + np.pi) % (2 * np.pi) - np.pi),
+                    abs(lnl[b] / rl - 1), int(rnp != npts[b])))
     same = np.array(m[True]).reshape(-1, 5)
     flip = np.array(m[False]).reshape(-1, 5)
+    rep = np.array(rep).reshape(-1, 5)
     out = {"vs": "FP64 oracle (CPU restatement, pinned to the reference's own code)",
-           "precision": "mixed" if precision else "f64", "sample": len(P), "skipped_status": skipped,
-           "same_end_sample": len(same), "end_sample_differs": len(flip)}
+           "precision": "mixed" if precision else "f64", "sample": len(P), "skipped_status": skipped}
+    if len(rep):
+        out["replay"] = {"how": "oracle integrated on the GPU's accepted knots (identical sampling)",
+                         "max_rel_row_error": float(rep[:, 0].max()),
+                         "max_strain_error_of_peak": float(rep[:, 1].max()),
+                         "max_dphi_at_peak_rad": float(rep[:, 2].max()),
+                         "max_rel_dlnl": float(rep[:, 3].max()), "median_rel_dlnl": float(np.median(rep[:, 3])),
+                         "frac_rel_dlnl_le_1e-9": float(np.mean(rep[:, 3] <= 1e-9)),
+                         "sample_count_differs": int(rep[:, 4].sum())}
+    free = {"how": "each side chooses its own steps", "same_end_sample": len(same),
+            "end_sample_differs": len(flip)}
     if len(same):
-        out.update({"max_dphi_at_peak_rad": float(same[:, 0].max()), "max_rel_amp_at_peak": float(same[:, 1].max()),
-                    "max_mismatch": float(same[:, 2].max()), "max_abs_dlnl": float(same[:, 3].max()),
-                    "max_rel_dlnl": float(same[:, 4].max()), "median_rel_dlnl": float(np.median(same[:, 4])),
-                    "frac_rel_dlnl_le_1e-9": float(np.mean(same[:, 4] <= 1e-9))})
+        free.update({"max_dphi_at_peak_rad": float(same[:, 0].max()), "max_rel_amp_at_peak": float(same[:, 1].max()),
+                     "max_mismatch": float(same[:, 2].max()), "max_abs_dlnl": float(same[:, 3].max()),
+                     "max_rel_dlnl": float(same[:, 4].max()), "median_rel_dlnl": float(np.median(same[:, 4])),
+                     "frac_rel_dlnl_le_1e-9": float(np.mean(same[:, 4] <= 1e-9))})
     if len(flip):
-        out["end_sample_differs_worst"] = {"max_mismatch": float(flip[:, 2].max()),
-                                           "max_abs_dlnl": float(flip[:, 3].max())}
+        free["end_sample_differs_worst"] = {"max_mismatch": float(flip[:, 2].max()),
+                                            "max_abs_dlnl": float(flip[:, 3].max())}
+    out["free_running"] = free
     return out
 
 
@@ -282,23 +312,33 @@ def run_reference(args, cfg, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
-            "config": config_block(cfg, args, extra={"sample": len(sample)}),
+            "config": config_block(cfg, args),
             "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": "port",
                              "sample": f"{len(sample)} of {cfg.batch} binaries (every {max(1, cfg.batch // n)}th), "
-                                       f"per step"},
+                                       f"per step; the oracle (CPU restatement of the reference path, pinned to "
+                                       f"the reference's own code), one process per core"},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
 
 
 def config_block(cfg, args, extra=None):
+    """The workload (the same for every arm)."""
     d = {"workload": f"config {cfg.index}: {cfg.name}", "batch": args.batch or cfg.batch,
          "total_mass_msun": list(cfg.total_mass), "mass_ratio": list(cfg.mass_ratio), "chi": list(cfg.chi),
          "f0_hz": list(cfg.f0), "modes": [list(m) for m in cfg.modes], "dt_s": cfg.dt, "n_samples": cfg.n_samples,
-         "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12, "queue": "longest first",
-         "l2": "flushed between timed steps (256 MiB write)",
-         "lanes_per_binary": getattr(args, "lanes", 0) or "auto",
+         "max_steps": args.max_steps, "rtol": 1e-12, "atol": 1e-12,
+         "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def impl_block(args, extra=None):
+    """How the native arm ran the workload."""
+    d = {"queue": "longest first", "lanes_per_binary": getattr(args, "lanes", 0) or "auto",
          "head_quads": "auto" if getattr(args, "head_quads", -1) < 0 else args.head_quads,
-         "integrator_block": getattr(args, "block", 0) or "default", "integrator_grid": getattr(args, "grid", 0) or "auto"}
+         "integrator_block": getattr(args, "block", 0) or "default",
+         "integrator_grid": getattr(args, "grid", 0) or "auto"}
     if extra:
         d.update(extra)
     return d
@@ -324,15 +364,14 @@ def census(args):
     print(json.dumps({"census": wl.counters()}))
 
 
-def run_plain(args, cfg, local):
-    """The plain FP64 GPU method for comparison: the reference's own launch
-    structure -- a host loop issuing the DOPR853 stages, error norm and
-    controller as separate launches per step (eob/new_Dormand_horiz.py:424-778,
-    src/DOPR853.cu:357-762) on top of the reference-shaped RHS kernels -- run
-    through the drop-in eob/ mirror on the same batch.  Only setup, initial
-    conditions and the two trajectory passes are timed (everything after the
-    trajectory costs under 1 % of the fused path), so its evals/s is an upper
-    bound for the plain method."""
+def run_refloop(args, cfg, local):
+    """The reference's own launch structure on the GPU: a host loop issuing the
+    DOPR853 stages, error norm and controller as separate launches per step
+    (eob/new_Dormand_horiz.py:424-778, src/DOPR853.cu:357-762) on top of the
+    reference-shaped RHS kernels, run through the drop-in eob/ mirror on the
+    same batch.  Only setup, initial conditions and the two trajectory passes
+    are timed (everything after the trajectory costs under 1 % of the fused
+    path), so its evals/s is an upper bound for that structure."""
     import torch
     from eobgpu_gb300.eob.seobnrv4phm import SEOBNRv4PHM
     device = torch.device(f"cuda:{local}")
@@ -359,11 +398,73 @@ def run_plain(args, cfg, local):
         times.append(time.perf_counter() - t0)
     tt = float(np.sum(times))
     B = len(params)
-    print(json.dumps({"impl": "plain", "metric": METRIC, "value": B * args.steps / tt, "unit": "evals/s",
+    print(json.dumps({"impl": "refloop", "metric": METRIC, "value": B * args.steps / tt, "unit": "evals/s",
                       "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 * tt / args.steps,
-                      "higher_is_better": True, "dtype": "f64",
-                      "config": config_block(cfg, args, extra={"timed": "setup + IC + two trajectory passes",
-                                                               "rows_max": int(ns.max().item())})}))
+                      "higher_is_better": True, "dtype": "f64", "config": config_block(cfg, args),
+                      "impl_config": {"timed": "setup + IC + two trajectory passes",
+                                      "rows_max": int(ns.max().item())}}))
+
+
+PLAIN_METHOD = ("plain FP64 GPU method: one warp (32 lanes) per binary, every binary on its own warp from the "
+                "start (grid = B / 4 blocks of 4 warps, queue in input order, no head of four-warp groups), "
+                "fused DOPR853 integrator + FP64 multipoles, splines, synthesis and lnL, eager launches, no "
+                "CUDA graph, no autotuning, one batch at a time")
+
+
+def plain_options(B):
+    """eob_options of the plain FP64 GPU method for a batch of B binaries."""
+    from eobgpu_gb300 import _lib
+    o = _lib.default_options()
+    o.lanes_per_binary = 32
+    o.head_quads = 0
+    o.precision = 0
+    o.block = 128
+    o.grid = max(1, -(-int(B) // 4))
+    return o
+
+
+def time_plain(P, D, cfg, amp, max_steps, device, steps, warmup, flush):
+    """The plain method on one batch: ms per step (CUDA events, L2 flushed
+    between steps) and the last lnL/status."""
+    import torch
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    B = int(P.shape[0])
+    wl = WaveformLikelihood(B, max_steps, list(cfg.modes), int(D.shape[0]), device=device, options=plain_options(B))
+    ident = torch.arange(B, dtype=torch.int32, device=device)
+    for _ in range(warmup):
+        wl.run(P, D, cfg.dt, amp, order=ident)
+    torch.cuda.synchronize()
+    ms = []
+    for i in range(steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lnl, st = wl.run(P, D, cfg.dt, amp, order=ident)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    out = (ms, lnl.cpu().numpy(), st.cpu().numpy())
+    del wl
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_plain(args, cfg, local):
+    """--impl plain: the plain FP64 GPU method alone on the workload's batch."""
+    import torch
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    params, data, amp = make_inputs(cfg, 0, device, args.max_steps)
+    P = torch.tensor(params, device=device)
+    D = torch.tensor(data, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    ms, _, st = time_plain(P, D, cfg, amp, args.max_steps, device, args.steps, args.warmup, flush)
+    t = float(np.sum(ms))
+    print(json.dumps({"impl": "plain", "metric": METRIC, "value": len(params) * args.steps / (t / 1e3),
+                      "unit": "evals/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": t / args.steps, "higher_is_better": True, "dtype": "f64",
+                      "config": config_block(cfg, args), "method": PLAIN_METHOD,
+                      "status_ok": int(np.sum(st == 0))}))
 
 
 OP_CENSUS = os.path.join(ROOT, "profiles", "tdinterp_fdlnl_fp64_census.md")
@@ -487,73 +588,132 @@ def run_op(args, local):
                       "l2": "flushed between timed launches (256 MiB write)"}))
 
 
-def run_serving(args, ws, rank, local):
-    """Configuration 4: a seeded Poisson trace of walker requests (1..512
-    binaries each, 80 % from a ball around the injection, 20 % from the
-    configuration-1 prior) replayed in wall-clock time through
-    LikelihoodServer.  The server's capacity is measured first (the whole
-    trace queued at once); the arrival rate is then set so that the offered
-    load is 70 % of that capacity.  Every rank replays its own trace."""
+def serving_measure(args, device, rank, ws, n_requests, precision=1, plain_sample=64, clocks=True):
+    """Configuration 4 on one GPU: a seeded Poisson trace of n_requests walker
+    requests (1..512 binaries each, 80 % from a ball around the injection,
+    20 % from the configuration-1 prior, dt = 1/1024 s, N = 8192) through
+    LikelihoodServer (continuous batching over concurrent slots, mixed
+    precision by default).
+
+    capacity -- the server saturated: the first min(n, 400) requests all
+      queued at t = 0; evals/s;
+    replay -- the whole trace replayed in wall-clock time at 70 % of that
+      capacity: request latency (completion minus arrival) p50/p99;
+    plain -- the plain FP64 GPU method serving the same requests one at a
+      time (each request one batch; host parameters in, lnL out, synchronous),
+      on every k-th request of the trace (plain_sample of them): evals/s."""
     import torch
+    from eobgpu_gb300.pipeline import WaveformLikelihood
     from eobgpu_gb300.serving import LikelihoodServer
     cfg = workload.CONFIGS[1]
+    max_steps = 4000
+    _, data, amp = make_inputs(cfg, rank, device, max_steps)
+    lanes = getattr(args, "lanes", 0) or 8
+    classes = [(1500, 1024, 2), (max_steps, 512, 1)]
+    server = LikelihoodServer(data, cfg.dt, amp, classes=classes, lanes_per_binary=lanes, precision=precision,
+                              head_quads=getattr(args, "head_quads", -1), device=device)
+    trace = workload.serving_trace(n_requests, 1.0, stream=rank)
+    for _ in range(2):
+        server.evaluate(trace.params[0])
+    npre = min(n_requests, 400)
+    sat = server.run_trace(np.zeros(npre), trace.params[:npre])
+    capacity = sat["binaries"] / sat["wall_s"]
+    sizes = np.array([len(np.atleast_2d(p)) for p in trace.params])
+    rate = 0.7 * capacity / float(np.mean(sizes))  # requests/s for 70 % of capacity
+    barrier(ws)
+    if clocks:
+        with ClockSampler(device.index if device.index is not None else 0) as clk:
+            res = server.run_trace(trace.arrivals, trace.params, time_scale=1.0 / rate)
+        clk_summary = clk.summary()
+    else:
+        res = server.run_trace(trace.arrivals, trace.params, time_scale=1.0 / rate)
+        clk_summary = None
+    ok = all(np.all(st == 0) for st in res["status"])
+    sts = np.concatenate([np.asarray(st) for st in res["status"]])
+    status_other = {str(int(v)): int(c) for v, c in zip(*np.unique(sts[sts != 0], return_counts=True))}
+    del server
+    torch.cuda.empty_cache()
+    # the plain FP64 GPU method on the same requests, one at a time
+    Dd = torch.tensor(data, device=device)
+    wl = WaveformLikelihood(512, max_steps, list(cfg.modes), cfg.n_samples, device=device, options=plain_options(512))
+    ident = torch.arange(512, dtype=torch.int32, device=device)
+    step = max(1, n_requests // plain_sample)
+    pick = list(range(0, n_requests, step))[:plain_sample]
+    host = [torch.from_numpy(np.ascontiguousarray(trace.params[i])).pin_memory() for i in pick]
+    out_h = torch.empty(512, dtype=torch.float64).pin_memory()
+    wl.options.grid = plain_options(len(host[0])).grid
+    wl.run(host[0].to(device), Dd, cfg.dt, amp, order=ident[:len(host[0])])
+    torch.cuda.synchronize()
+    t_plain = 0.0
+    n_plain = 0
+    for hp in host:
+        n = int(hp.shape[0])
+        wl.options.grid = plain_options(n).grid
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        l_d, _ = wl.run(hp.to(device, non_blocking=True), Dd, cfg.dt, amp, order=ident[:n])
+        out_h[:n].copy_(l_d, non_blocking=True)
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t0
+        n_plain += n
+    del wl
+    torch.cuda.empty_cache()
+    plain = n_plain / t_plain
+    out = {"workload": "config 4: serving, continuous batching over concurrent slots",
+           "requests": n_requests, "request_size": [1, 512], "binaries": int(res["binaries"]),
+           "precision": "mixed (f64 integrator, phase and spline solve; f32 amplitude, sincos, residual)"
+                        if precision else "f64",
+           "capacity": {"value": capacity, "unit": "evals/s",
+                        "how": f"first {npre} requests all queued at t = 0 (saturated server)",
+                        "slot_busy_fraction": sat["slot_busy_fraction"]},
+           "replay": {"rate_hz": rate, "offered_load": "70 % of the measured capacity",
+                      "throughput": res["binaries"] / res["wall_s"], "wall_s": res["wall_s"],
+                      "latency_ms": {"p50": res["p50_ms"], "p99": res["p99_ms"]},
+                      "slot_busy_fraction": res["slot_busy_fraction"], "batches": res["batches"],
+                      "requeued": res["requeued"], "status_ok": bool(ok), "status_other": status_other},
+           "plain": {"value": plain, "unit": "evals/s", "method": PLAIN_METHOD,
+                     "sample": f"{len(pick)} requests (every {step}th), {n_plain} binaries, one request at a time, "
+                               f"host parameters in and lnL out per request"},
+           "served_vs_plain": capacity / plain, "target_served_vs_plain": 5.0,
+           "classes_max_steps_batch_slots": classes, "lanes_per_binary": lanes,
+           "admission": "by estimated trajectory rows (chirp-time fit x3), re-run on overflow",
+           "dt_s": cfg.dt, "n_samples": cfg.n_samples}
+    if clk_summary is not None:
+        out["clocks"] = clk_summary
+    return out, res, sat
+
+
+def run_serving(args, ws, rank, local):
+    """--config 4: the serving workload alone, one JSON line (every rank
+    replays its own trace)."""
+    import torch
     device = torch.device(f"cuda:{local}")
     torch.cuda.set_device(device)
-    _, data, amp = make_inputs(cfg, rank, device, args.max_steps)
-    lanes = args.lanes or 8
-    classes = [(1500, 1024, 2), (args.max_steps, 512, 1)]
-    server = LikelihoodServer(data, cfg.dt, amp, classes=classes, lanes_per_binary=lanes,
-                              precision=0 if args.fp64 else 1, head_quads=args.head_quads, device=device)
-    trace = workload.serving_trace(args.requests, 1.0, stream=rank)
-    for _ in range(args.warmup):
-        server.evaluate(trace.params[0])
-    # capacity: the same requests all queued at t = 0 (the server saturated)
-    sat = server.run_trace(np.zeros(len(trace.params)), trace.params)
-    capacity = sat["binaries"] / sat["wall_s"]
-    mean_size = float(np.mean([len(np.atleast_2d(p)) for p in trace.params]))
-    rate = 0.7 * capacity / mean_size  # requests/s for 70 % of capacity
-    barrier(ws)
-    results = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            results.append(server.run_trace(trace.arrivals, trace.params, time_scale=1.0 / rate))
-    clocks = clk.summary()
-    wall = max_over_ranks(float(sum(r["wall_s"] for r in results)), ws, device)
-    nbin = sum(r["binaries"] for r in results) * ws
-    lat = np.concatenate([r["latency_s"] for r in results])
-    ok = all(np.all(st == 0) for r in results for st in r["status"])
+    sv, res, sat = serving_measure(args, device, rank, ws, args.requests, precision=0 if args.fp64 else 1)
+    wall = max_over_ranks(float(res["wall_s"]), ws, device)
+    nbin = res["binaries"] * ws
     if rank == 0:
-        accuracy = None
-        if args.accuracy_sample > 0:
-            allp = np.concatenate([np.atleast_2d(p) for p in trace.params])
-            accuracy = accuracy_vs_oracle(allp, cfg, data, amp, args.max_steps, 0 if args.fp64 else 1, device,
-                                          args.accuracy_sample, os.cpu_count() or 1)
         value = nbin / wall
-        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": 1,
+                "warmup": args.warmup, "ms_per_step": 1e3 * wall, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.fp64 else "f64 integrator; f64 phase + f32 amplitude/sincos/residual synthesis",
                 "data": "synthetic: seeded Poisson trace of walker requests, white noise + one injection at SNR 30",
-                "config": {"workload": "config 4: serving, continuous batching over concurrent slots",
-                           "requests": args.requests, "request_size": [1, 512], "rate_hz": rate,
-                           "offered_load": "70 % of the measured capacity", "classes_max_steps_batch_slots": classes,
-                           "admission": "by estimated trajectory rows (chirp-time fit x3), re-run on overflow",
-                           "requeued": int(sum(r["requeued"] for r in results)), "lanes_per_binary": lanes,
-                           "head_quads": "auto" if args.head_quads < 0 else args.head_quads,
-                           "max_steps": args.max_steps, "dt_s": cfg.dt, "n_samples": cfg.n_samples,
+                "config": {"workload": sv["workload"], "requests": args.requests, "request_size": [1, 512],
+                           "dt_s": sv["dt_s"], "n_samples": sv["n_samples"],
                            "l2": "inputs of each batch are new; no flush (latency run)"},
-                "e2e": {"value": value, "unit": "evals/s",
-                        "h2d_bytes_per_step": int(nbin / ws / args.steps * 40),
-                        "d2h_bytes_per_step": int(nbin / ws / args.steps * 12)},
-                "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
-                "slot_busy_fraction": float(np.mean([r["slot_busy_fraction"] for r in results])),
-                "capacity": {"value": capacity, "unit": "evals/s",
-                             "how": "the same requests all queued at t = 0 (saturated server)",
-                             "slot_busy_fraction": sat["slot_busy_fraction"]},
-                "batches": int(sum(r["batches"] for r in results)),
-                "gpu_launches": int(8 * sum(r["batches"] for r in results)),
-                "roofline": None, "cpu_baseline": None, "clocks": clocks, "status_ok": bool(ok),
-                "accuracy": accuracy}
+                "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": int(nbin / ws * 40),
+                        "d2h_bytes_per_step": int(nbin / ws * 12)},
+                "latency_ms": sv["replay"]["latency_ms"], "serving": sv,
+                "gpu_launches": int(8 * res["batches"]), "roofline": None, "cpu_baseline": None,
+                "clocks": sv.get("clocks"), "status_ok": sv["replay"]["status_ok"]}
+        if args.accuracy_sample > 0:
+            cfg = workload.CONFIGS[1]
+            _, data, amp = make_inputs(cfg, rank, device, 4000)
+            trace = workload.serving_trace(args.requests, 1.0, stream=rank)
+            allp = np.concatenate([np.atleast_2d(p) for p in trace.params])
+            line["accuracy"] = accuracy_vs_oracle(allp, cfg, data, amp, 4000, 0 if args.fp64 else 1, device,
+                                                  args.accuracy_sample, os.cpu_count() or 1)
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
@@ -565,10 +725,15 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="native", choices=["native", "reference", "plain"])
+    ap.add_argument("--impl", default="native", choices=["native", "reference", "plain", "refloop"])
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--fp64", action="store_true", help="configuration 3 in FP64 instead of mixed precision")
     ap.add_argument("--requests", type=int, default=2000, help="configuration 4: requests in the trace")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving block (configuration 4 trace) of the default line")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 GPU method on the same batch in the default line")
+    ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain method in the default line")
     ap.add_argument("--head", type=int, default=0,
                     help="configuration 5: longest binaries run concurrently on their own workspace (-1: B/50)")
     ap.add_argument("--slots", type=int, default=1, help="configuration 5: concurrent chunk workspaces")
@@ -613,6 +778,9 @@ def main():
     ws, rank, local = dist_init()
     if args.impl == "plain":
         run_plain(args, cfg, local)
+        return
+    if args.impl == "refloop":
+        run_refloop(args, cfg, local)
         return
     if args.op:
         run_op(args, local)
@@ -772,6 +940,20 @@ def main():
                 "work": f"{F_RHS:.0f} FP64 FLOP per RHS x {cnt['rhs_binaries']} RHS evaluations",
                 "lane_occupancy": cnt["rhs_binaries"] / max(1, cnt["rhs_all_lanes"])}
 
+    # ---- the plain FP64 GPU method on the same batch, and the serving
+    # workload (configuration 4 trace), one GPU only
+    plain_block = None
+    if ws == 1 and chunked is None and not args.no_plain:
+        pms, plnl, pst = time_plain(P, D, cfg, amp, args.max_steps, device, max(1, args.plain_steps), 1, flush)
+        pt = float(np.sum(pms))
+        plain_block = {"value": B * len(pms) / (pt / 1e3), "unit": "evals/s", "ms_per_step": pt / len(pms),
+                       "steps": len(pms), "warmup": 1, "method": PLAIN_METHOD,
+                       "status_ok": int(np.sum(pst == 0)),
+                       "max_rel_dlnl_vs_this_run": float(np.max(np.abs(plnl / lnl.cpu().numpy() - 1)))}
+    serving = None
+    if ws == 1 and args.config == 2 and not args.batch and not args.no_serving:
+        serving, _, _ = serving_measure(args, device, rank, ws, args.requests)
+
     graphed = chunked is None and not args.no_graph
     extra_cfg = {"cuda_graph": graphed}
     if chunked is not None:
@@ -802,13 +984,20 @@ def main():
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64 integrator; f64 phase + f32 amplitude/sincos/residual synthesis" if mixed else "f64",
                 "data": "synthetic: seeded parameters, white noise + one injection at SNR 30",
-                "config": config_block(cfg, args, extra=extra_cfg),
+                "config": config_block(cfg, args), "impl_config": impl_block(args, extra=extra_cfg),
                 "e2e": {"value": e2e_value, "unit": "evals/s",
                         "h2d_bytes_per_step": int(B * 5 * 8 + (0 if graphed else B * 4)),
                         "d2h_bytes_per_step": int(B * 8 + B * 4)},
                 "roofline": roof, "cpu_baseline": cpu_base, "clocks": clocks,
                 "gpu_launches": launches_per_step * args.steps,
-                "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+                "latency_ms": (dict(serving["replay"]["latency_ms"], source="request latency of the serving "
+                               "block (2000-request Poisson trace at 70 % load)") if serving else
+                               {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                                "source": "timed steps of this batch"}),
+                "step_latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                                    "p99": float(np.percentile(step_ms, 99))},
+                "plain": plain_block, "vs_plain": (value / plain_block["value"]) if plain_block else None,
+                "serving": serving,
                 "stages_ms": stage_ms, "stages_batch": Bst, "critical_path": critical,
                 "fp64_peak_tflops": fp64_peak,
                 "status_ok": int(np.sum(status == 0)),

@@ -174,6 +174,19 @@ class OracleContext:
         self.o.lib.oracle_ctx_ode(self.h, _dp(state), _dp(k), _dp(add), ctypes.c_int(n), _ip(idx))
         return k
 
+    def waveform(self, r, phi, pr, pphi, v, Hreal, eta, vPhi, l, m, prefix, h22_calib=0.0):
+        """EOBGetSpinFactorizedWaveform for binary 0 of this context over one
+        trajectory (src/EOB.cu:1235-1613): complex h_lm per row."""
+        r, phi, pr, pphi, v, Hreal, vPhi = map(_f64, (r, phi, pr, pphi, v, Hreal, vPhi))
+        n = len(r)
+        out = np.zeros(2 * n)
+        pre = _f64([np.real(prefix), np.imag(prefix)])
+        idx = np.zeros(1, dtype=np.int32)
+        self.o.lib.oracle_ctx_waveform(self.h, _dp(out), _dp(r), _dp(phi), _dp(pr), _dp(pphi), _dp(v), _dp(Hreal),
+                                       _dp(_f64([eta])), _dp(vPhi), ctypes.c_int(l), ctypes.c_int(m), _dp(pre),
+                                       ctypes.c_double(h22_calib), ctypes.c_int(1), ctypes.c_int(n), _ip(idx))
+        return out[0::2] + 1j * out[1::2]
+
     def rr_force(self, state, add, idx=None):
         state, add = _f64(state), _f64(add)
         n = state.shape[1]

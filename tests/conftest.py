@@ -25,4 +25,4 @@ def oracle():
 def golden():
     import numpy as np
     d = os.path.join(HERE, "golden")
-    return {k: dict(np.load(os.path.join(d, k + ".npz"))) for k in ("ham_rhs", "fac_coeffs", "spline", "config1")}
+    return {k: dict(np.load(os.path.join(d, k + ".npz"))) for k in ("ham_rhs", "fac_coeffs", "spline", "config1", "modes5")}

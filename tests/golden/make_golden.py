@@ -273,8 +273,10 @@ class RefBinary:
         L = S + 1
         return t[:L].copy(), traj[:L].copy(), S
 
-    def modes(self, t, traj, ells, mms):
-        """get_hlms, eob/seobnrv4phm.py:2138-2221 -> complex[K][L]."""
+    def modes(self, t, traj, ells, mms, inputs=None):
+        """get_hlms, eob/seobnrv4phm.py:2138-2221 -> complex[K][L]; `inputs`
+        (a dict, if given) receives the per-row v, H_real and vPhi passed to
+        EOBGetSpinFactorizedWaveform."""
         lib = self.ref.lib
         L = len(t)
         r, phi, pr, pphi = [np.ascontiguousarray(traj[:, j]) for j in range(4)]
@@ -300,6 +302,8 @@ class RefBinary:
                                  dp(np.array([nu])), dp(vPhi), ctypes.c_int(l), ctypes.c_int(m), dp(pk),
                                  ctypes.c_double(0.0), ctypes.c_int(1), ctypes.c_int(L), ip(self.idx))
             out[j] = tmp[0::2] + 1j * tmp[1::2]
+        if inputs is not None:
+            inputs.update({"v": v, "Hreal": Hval, "vPhi": vPhi, "eta": nu})
         return out
 
 
@@ -352,13 +356,63 @@ def synthesize(ref: Ref, t_M, traj, hlms, mms, mt, dt):
 
 
 # ---------------------------------------------------------------------------
+def make_modes5(ref: Ref, max_step: int):
+    """Every mode the reference's waveform class computes, (2,2), (2,1), (3,3),
+    (4,4), (5,5) (eob/seobnrv4phm.py:1869), for the eight configuration-1
+    binaries (unequal masses, q 1-3): EOBGetSpinFactorizedWaveform on the
+    reference's own trajectories (src/EOB.cu:1235-1677) with the per-row
+    inputs it was given, the five-mode strain on the uniform grid and the
+    five-mode likelihood against the configuration-1 data."""
+    cfg = workload.CONFIGS[1]
+    c1 = dict(np.load(os.path.join(HERE, "config1.npz")))
+    modes = workload.ALL_MODES
+    ells = [l for l, _ in modes]
+    mms = [m for _, m in modes]
+    params = c1["params"]
+    data, amp, N = c1["data"], float(c1["amp"]), int(c1["N"])
+    L = int(c1["nsteps"].max())
+    B = len(params)
+    out = {"modes": np.array(modes), "params": params, "nsteps": c1["nsteps"], "traj_t": c1["traj_t"],
+           "traj_y": c1["traj_y"], "hlm": np.zeros((B, 5, L), dtype=np.complex128), "v": np.zeros((B, L)),
+           "Hreal": np.zeros((B, L)), "vPhi": np.zeros((B, L)), "eta": np.zeros(B), "prefix": np.zeros((B, 5),
+                                                                                                        dtype=complex),
+           "lnl": np.zeros(B), "npts": np.zeros(B, dtype=int)}
+    for b, p in enumerate(params):
+        n = int(c1["nsteps"][b])
+        t, traj = c1["traj_t"][b, :n], c1["traj_y"][b, :n]
+        rb = RefBinary(ref, p[0], p[1], p[2], p[3], p[4], max_step)
+        inp = {}
+        hl = rb.modes(t, traj, ells, mms, inputs=inp)
+        hs, npts = synthesize(ref, t, traj, hl, mms, p[0] + p[1], cfg.dt)
+        out["prefix"][b] = [rb.prefixes_hlms[(l - 2) * (l + 1) // 2 + (m - 1)] for l, m in modes]
+        rb.close()
+        out["hlm"][b, :, :n] = hl
+        for k in ("v", "Hreal", "vPhi"):
+            out[k][b, :n] = inp[k]
+        out["eta"][b] = inp["eta"]
+        h = np.zeros(N)
+        m = min(npts, N)
+        h[:m] = amp * hs[:m].real
+        out["lnl"][b] = -0.5 * np.sum((data - h) ** 2)
+        out["npts"][b] = npts
+        out[f"h_{b}"] = hs[:N]
+        print(f"binary {b}: q={p[0] / p[1]:.3f} rows={n} npts={npts} lnL(5 modes)={out['lnl'][b]:.6f}")
+    np.savez_compressed(os.path.join(HERE, "modes5.npz"), **out)
+    print("modes5.npz written")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--max-step", type=int, default=20000)
+    ap.add_argument("--only", choices=["modes5"], default=None,
+                    help="write only this fixture (modes5 needs config1.npz)")
     args = ap.parse_args()
     subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh"), args.ref])
     ref = Ref(os.path.join(ROOT, "oracle", "_ref", "libeobref.so"))
+    if args.only == "modes5":
+        make_modes5(ref, args.max_step)
+        return
     out = {}
 
     # (1) Hamiltonian, gradient, Hessian, ODE RHS and RR force on random states
@@ -485,6 +539,7 @@ def main():
         res[f"h_{b}"] = hsum[b]
     np.savez_compressed(os.path.join(HERE, "config1.npz"), **res)
     print("config1.npz written")
+    make_modes5(ref, args.max_step)
 
 
 if __name__ == "__main__":
