@@ -77,6 +77,10 @@ _SIGS = {
     "eob_tdinterp2": (c_int, [_P] * 7 + [c_int, _P, c_int, c_int, c_int, _P, _P, _P, _P, c_int, _P]),
     "eob_tdinterp": (c_int, [_P] * 8 + [c_int, c_int, c_int, _P, _P, _P, _P, _P, _P]),
     "eob_all_in_one_likelihood": (c_int, [_P] * 8 + [c_double, c_int, c_int, c_int, _P]),
+    "eob_detector_response": (c_int, [_P] * 6 + [c_int, c_int, _P, _P, _P, _P]),
+    "eob_fd_lnl_scratch_bytes": (c_size_t, [c_int, c_int]),
+    "eob_fd_lnl_from_fft": (c_int, [_P, c_int, c_int, _P, _P, _P, _P, _P, c_double, c_int, c_int, _P, c_size_t, _P,
+                                    _P]),
 }
 
 _lib = None

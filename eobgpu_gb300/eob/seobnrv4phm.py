@@ -27,6 +27,7 @@ import numpy as np
 import torch
 
 from .. import _lib
+from .. import fd as fdm
 from ..pipeline import WaveformLikelihood, longest_first
 from . import pyEOB, pytdinterp
 from .new_Dormand_horiz import DOPR853
@@ -415,37 +416,117 @@ class SEOBNRv4PHM:
 
 
 class BBHWaveformTD:
-    """Mode-summed strain and likelihood (eob/seobnrv4phm.py:503-823).
+    """Mode-summed strain, detector response and likelihood
+    (eob/seobnrv4phm.py:503-823).
 
-    `return_type="geocenter_td"` returns sum_lm h_lm on the uniform grid
-    (plus = real, cross = imaginary); `get_ll_td` is the white-noise
-    time-domain likelihood of this build.  Detector projection and the
-    frequency-domain likelihood need bilby interferometers and are not part of
-    this path."""
+    bilby_interferometers: objects with bilby's detector_tensor,
+    geometry.vertex, strain_data.start_time, amplitude_spectral_density_array
+    and frequency_domain_strain (eobgpu_gb300.fd.Interferometer provides them
+    without bilby).  return_type "geocenter_td" (sum_lm h_lm on the uniform
+    grid, plus = real, cross = imaginary), "geocenter_fd" (its two real FFTs),
+    "detector_fd" (projected onto each detector with its delay) or "like"
+    (returns None, as the reference); get_ll is the reference's likelihood;
+    get_ll_td the white-noise time-domain likelihood of this build.  Each
+    binary's template is zero past its own end (the reference's batched
+    synthesis holds the last value up to the batch's longest waveform; a
+    single-binary call gives zero)."""
 
     def __init__(self, bilby_interferometers=None, amp_phase_kwargs={}, interp_kwargs={}, use_gpu=True):
         self.amp_phase_gen = SEOBNRv4PHM(**amp_phase_kwargs)
+        self.use_gpu = True
         self.bilby_interferometers = bilby_interferometers
+        self.num_interp_params = 2
+        if bilby_interferometers is not None:
+            ifos = list(bilby_interferometers)
+            self.detector_tensors = _cuda(np.array([bi.detector_tensor for bi in ifos]))
+            self.detector_start_times = _cuda(np.array([bi.strain_data.start_time for bi in ifos]))
+            self.detector_vertex = _cuda(np.array([bi.geometry.vertex for bi in ifos]))
+            psd = np.array([np.asarray(bi.amplitude_spectral_density_array) ** 2 for bi in ifos]).flatten()
+            psd[np.isinf(psd)] = 1e300
+            self.psd = _cuda(psd)
+            data = np.array([bi.frequency_domain_strain for bi in ifos], dtype=np.complex128)
+            self.fd_data_length = data.shape[1]
+            self.nChannels = data.shape[0]
+            self.data = _cuda(data.flatten(), torch.complex128)
+        self._fd = None
 
-    def __call__(self, m1, m2, chi1z, chi2z, distance, phiRef, inc=None, ra=None, dec=None, psi=None,
-                 geocent_time=None, sampling_frequency=1024, Tobs=60.0, modes=None, bufferSize=None, fill=False,
-                 fs=20.0, return_type="geocenter_td", combine_modes=True, bilby_start_ind=0):
-        if return_type != "geocenter_td":
-            raise NotImplementedError("only return_type='geocenter_td' (detector projection and the FD likelihood "
-                                      "are outside this path)")
-        N = int(Tobs * sampling_frequency)
+    def get_detector_information(self, ra, dec, time, psi):
+        """(F+, Fx, delay from the geocenter) [nch, B] (eob/seobnrv4phm.py:597-634)."""
+        self._need_ifos()
+        return fdm.detector_response(ra, dec, psi, time, self.detector_tensors, self.detector_vertex)
+
+    def _need_ifos(self):
+        if self.bilby_interferometers is None:
+            raise ValueError("Must provide detector_tensors kwarg.")
+
+    def _templates(self, m1, m2, chi1z, chi2z, distance, modes, fs, N, dt):
         gen = self.amp_phase_gen
         m1 = _cuda(m1).reshape(-1)
         B = m1.numel()
+        self.num_bin_all = B
         ells = gen.ells_default if modes is None else np.asarray([l for l, _ in modes], dtype=np.int32)
         mms = gen.mms_default if modes is None else np.asarray([m for _, m in modes], dtype=np.int32)
-        wl = WaveformLikelihood(B, gen.max_step, [(int(l), int(m)) for l, m in zip(ells, mms)], N,
-                                options=gen.options)
-        params = torch.stack([m1, _cuda(m2).reshape(-1), _cuda(chi1z).reshape(-1), _cuda(chi2z).reshape(-1),
-                              _cuda(fs).expand(B)], dim=1).contiguous()
-        h, st = wl.strain(params, 1.0 / sampling_frequency, N)
+        self.num_modes = len(ells)
+        lm = [(int(l), int(m)) for l, m in zip(ells, mms)]
+        key = (B, tuple(lm), N)
+        if getattr(self, "_wl_key", None) != key:
+            self._wl = WaveformLikelihood(B, gen.max_step, lm, N, options=gen.options)
+            self._wl_key = key
+        fsv = _cuda(fs).expand(B) if np.ndim(fs) == 0 else _cuda(fs).reshape(-1)
+        params = torch.stack([m1, _cuda(m2).reshape(-1), _cuda(chi1z).reshape(-1), _cuda(chi2z).reshape(-1), fsv],
+                             dim=1).contiguous()
+        h, st = self._wl.strain(params, dt, N, order=longest_first(params))
         self.status = st
         return h / _cuda(distance).reshape(-1)[:, None]
+
+    def __call__(self, m1, m2, chi1z, chi2z, distance, phiRef, inc=None, ra=None, dec=None, psi=None,
+                 geocent_time=None, sampling_frequency=1024, Tobs=60.0, modes=None, bufferSize=None, fill=False,
+                 fs=20.0, return_type="like", combine_modes=True, bilby_start_ind=0):
+        if return_type not in ("geocenter_td", "geocenter_fd", "detector_td", "detector_fd", "like"):
+            raise ValueError("return_type must be geocenter_td, geocenter_fd, like, or detector_fd.")
+        self.sampling_frequency = sampling_frequency
+        self.data_length = N = int(Tobs * sampling_frequency)
+        h = self._templates(m1, m2, chi1z, chi2z, distance, modes, fs, N, 1.0 / sampling_frequency)
+        if return_type == "geocenter_td":
+            return h
+        hp, hc = fdm.split_real_ffts(torch.fft.fft(h, dim=-1))
+        hp[:, :bilby_start_ind] = 0.0
+        hc[:, :bilby_start_ind] = 0.0
+        self.templates_out = [hp, hc]
+        if return_type == "geocenter_fd":
+            return hp, hc
+        Fplus, Fcross, time_shift = self.get_detector_information(ra, dec, geocent_time, psi)
+        if return_type == "detector_td":
+            raise NotImplementedError
+        if return_type == "detector_fd":
+            f = torch.fft.rfftfreq(N, 1.0 / sampling_frequency, dtype=torch.float64, device="cuda")
+            return ((Fplus.T[:, :, None] * hp[:, None, :] + Fcross.T[:, :, None] * hc[:, None, :])
+                    * torch.exp(-2j * np.pi * f[None, None, :] * time_shift.T[:, :, None]))
+        return None
+
+    def get_ll(self, params, sampling_frequency=1024, return_complex=False, return_cupy=False, Tobs=60.0,
+               modes=None, fs=20.0, bilby_start_ind=0, **kwargs):
+        """lnL per binary for params = (m1, m2, chi1z, chi2z, distance, phiRef,
+        inc, ra, dec, psi, geocent_time), each of length B
+        (eob/seobnrv4phm.py:772-823)."""
+        self._need_ifos()
+        m1, m2, chi1z, chi2z, distance, phiRef, inc, ra, dec, psi, geocent_time = params
+        self.sampling_frequency = sampling_frequency
+        self.data_length = N = int(Tobs * sampling_frequency)
+        if N // 2 + 1 != self.fd_data_length:
+            raise ValueError(f"Tobs x sampling_frequency = {N} samples do not match the data's "
+                             f"{self.fd_data_length} frequency bins")
+        h = self._templates(m1, m2, chi1z, chi2z, distance, modes, fs, N, 1.0 / sampling_frequency)
+        H = torch.fft.fft(h, dim=-1)
+        del h
+        Fplus, Fcross, time_shift = self.get_detector_information(ra, dec, geocent_time, psi)
+        df = 1.0 / (N / sampling_frequency)
+        like = fdm.fd_lnl_from_fft(torch.view_as_real(H).contiguous(), self.data.view(self.nChannels, -1),
+                                   self.psd.view(self.nChannels, -1), Fplus, Fcross, time_shift, df,
+                                   bilby_start_ind)
+        if return_complex:
+            like = like.to(torch.complex128)
+        return like if return_cupy else like.cpu().numpy()
 
     def get_ll_td(self, params, data, amp, sampling_frequency=1024, modes=None, fs=20.0):
         """lnL = -1/2 sum_k (d_k - amp Re sum_lm h_lm(t_k))^2 for params[B, 4] (m1, m2, chi1z, chi2z)."""

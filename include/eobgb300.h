@@ -253,6 +253,35 @@ int eob_all_in_one_likelihood(double *temp_sum, const double *hp_fd, const doubl
                               double df, int num_bin_all, int nchannels, int data_length, cudaStream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Frequency-domain likelihood (BBHWaveformTD.get_ll, eob/seobnrv4phm.py:772-823)
+ */
+
+/* Detector response, eob/seobnrv4phm.py:597-634 (get_detector_information):
+ * per binary b (ra, dec, psi [rad], geocent_time [GPS s]) and detector c
+ * (detector_tensors[c][3][3], vertices[c][3] in m, Earth-fixed), the antenna
+ * patterns Fplus/Fcross[c * B + b] and the delay from the geocenter
+ * time_shift[c * B + b] [s].  The Greenwich mean sidereal time (the
+ * reference calls lal through bilby) is the IAU 1982 expression of the GPS
+ * time with GPS - UTC leap seconds to 2017 and UT1 = UTC.  Device arrays. */
+int eob_detector_response(const double *ra, const double *dec, const double *psi, const double *geocent_time,
+                          const double *detector_tensors, const double *vertices, int B, int nch, double *Fplus,
+                          double *Fcross, double *time_shift, cudaStream_t stream);
+/* The likelihood of eob/seobnrv4phm.py:736-744 + 778-817 from H[b][k] (complex,
+ * interleaved), the complex FFT over N (even) samples of each binary's summed
+ * strain h_+ + i h_x: the two real FFTs of the reference are recovered as
+ * h~_+(f) = (H(f) + conj H(N-f)) / 2 and h~_x(f) = (H(f) - conj H(N-f)) / 2i for
+ * the N/2 + 1 bins f = k df, set to zero below start_ind (bilby_start_ind);
+ * lnl[b] = -1/2 4 df sum_c sum_f |d_c(f) - (F+ h~_+ + Fx h~_x) e^{-2 pi i f tau}|^2
+ * / psd_c(f) with data[c][N/2 + 1] (complex), psd[c][N/2 + 1], Fplus, Fcross,
+ * time_shift[c * B + b] (the all_in_one_likelihood partials,
+ * src/interpolate.cu:551-627, summed).  nch <= 8.  scratch: device memory of
+ * eob_fd_lnl_scratch_bytes(B, N) bytes. */
+size_t eob_fd_lnl_scratch_bytes(int B, int N);
+int eob_fd_lnl_from_fft(const double *H, int N, int start_ind, const double *data, const double *psd,
+                        const double *Fplus, const double *Fcross, const double *time_shift, double df, int B, int nch,
+                        void *scratch, size_t scratch_bytes, double *lnl, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Measurement and test hooks.  Not part of the waveform path and without a
  * counterpart in the reference: they exist so that the benchmark can measure
  * its roofline denominator on the device it runs on and the tests can check

@@ -194,3 +194,12 @@ class OracleContext:
         f = np.zeros((2, n))
         self.o.lib.oracle_ctx_rr_force(self.h, _dp(f), _dp(state), _dp(add), ctypes.c_int(n), _ip(idx))
         return f
+
+
+def detail_job(job):
+    """One whole-path oracle run for a process pool (start the pool with the
+    'spawn' method): job = (params, dt, N, modes, data, amp, max_step,
+    replay_t or None).  Returns lnl, status, nsteps, npts, h."""
+    params, dt, N, modes, data, amp, max_step, replay_t = job
+    r = Oracle().lnl_one(params, dt, N, modes, data, amp, max_step=max_step, want_detail=True, replay_t=replay_t)
+    return {k: r[k] for k in ("lnl", "status", "nsteps", "npts", "h")}

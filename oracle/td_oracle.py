@@ -102,3 +102,64 @@ def tdinterp_inputs(dataTime, t_shaped, lengths):
         inds[b * max_length + st[b]: b * max_length + et[b]] = (
             np.searchsorted(t_shaped[b], dataTime[st[b]:et[b]], side="right").astype(np.int32) - 1)
     return lens, inds, max_length
+
+
+# ---------------------------------------------------------------------------
+# Detector response and the frequency-domain get_ll flow (numpy restatement)
+SPEED_OF_LIGHT = 299792458.0
+# GPS times at which GPS - UTC grew by one second (1981-07-01 ... 2017-01-01 UTC)
+LEAP_GPS = np.array([46828801, 78364802, 109900803, 173059204, 252028805, 315187206, 346723207, 393984008,
+                     425520009, 457056010, 504489611, 551750412, 599184013, 820108814, 914803215, 1025136016,
+                     1119744017, 1167264018], dtype=np.float64)
+
+
+def gmst_from_gps(gps):
+    """Greenwich mean sidereal time [rad] (IAU 1982, UT1 = UTC), the quantity
+    the reference takes from lal through bilby (eob/seobnrv4phm.py:600-601)."""
+    gps = np.asarray(gps, dtype=np.float64)
+    leap = np.sum(gps[..., None] >= LEAP_GPS, axis=-1)
+    days = (gps - leap) / 86400.0 - (2451545.0 - 2444244.5)
+    T = days / 36525.0
+    s = 67310.54841 + T * ((876600.0 * 3600.0 + 8640184.812866) + T * (0.093104 - 6.2e-6 * T))
+    s = np.mod(s, 86400.0)
+    return s * (2.0 * np.pi / 86400.0)
+
+
+def detector_information(ra, dec, time, psi, detector_tensors, detector_vertex):
+    """get_detector_information (eob/seobnrv4phm.py:597-634): F+, Fx and the
+    delay from the geocenter, each [nch, B]."""
+    gmst = np.fmod(gmst_from_gps(time), 2 * np.pi)
+    phi = np.asarray(ra) - gmst
+    theta = np.pi / 2 - np.asarray(dec)
+    psi = np.asarray(psi)
+    u = np.array([np.cos(phi) * np.cos(theta), np.cos(theta) * np.sin(phi), -np.sin(theta)]).T
+    v = np.array([-np.sin(phi), np.cos(phi), np.zeros_like(phi)]).T
+    m = -u * np.sin(psi)[:, None] - v * np.cos(psi)[:, None]
+    n = -u * np.cos(psi)[:, None] + v * np.sin(psi)[:, None]
+    ep = np.einsum("...i,...j->...ij", m, m) - np.einsum("...i,...j->...ij", n, n)
+    ex = np.einsum("...i,...j->...ij", m, n) + np.einsum("...i,...j->...ij", n, m)
+    Fp = np.einsum("kij,lij->kl", detector_tensors, ep)
+    Fx = np.einsum("kij,lij->kl", detector_tensors, ex)
+    omega = np.array([np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), np.cos(theta)]).T
+    tau = np.einsum("ij,kj->ki", omega, detector_vertex) / SPEED_OF_LIGHT
+    return Fp, Fx, tau
+
+
+def fd_get_ll(h_td, data, psd, ra, dec, psi, time, detector_tensors, detector_vertex, sampling_frequency,
+              start_ind=0):
+    """The rest of get_ll (eob/seobnrv4phm.py:736-744, 778-817) from the summed
+    time-domain strain h_td [B, N] (complex: plus = real, cross = imaginary):
+    two real FFTs, bins below start_ind zeroed, detector projection, PSD-
+    weighted residual, lnL = -1/2 df 4 sum.  data, psd: [nch, N/2 + 1]."""
+    B, N = h_td.shape
+    nch = data.shape[0]
+    hp = np.fft.rfft(h_td.real, axis=-1)
+    hc = np.fft.rfft(h_td.imag, axis=-1)
+    hp[:, :start_ind] = 0.0
+    hc[:, :start_ind] = 0.0
+    Fp, Fx, tau = detector_information(ra, dec, time, psi, detector_tensors, detector_vertex)
+    Nf = hp.shape[1]
+    df = 1.0 / (N / sampling_frequency)
+    temp = all_in_one_likelihood(hp.ravel(), hc.ravel(), data.ravel(), psd.ravel(), Fp.ravel(), Fx.ravel(),
+                                 tau.ravel(), df, B, nch, Nf)
+    return fd_lnl(temp, df, B, nch).real
