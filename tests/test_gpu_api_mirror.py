@@ -61,7 +61,7 @@ def test_bbh_td_strain_and_likelihood(torch_cuda, golden):
     N = int(c["N"])
     bbh = BBHWaveformTD(None, amp_phase_kwargs={"max_step": 4096})
     h = bbh(P[:2, 0], P[:2, 1], P[:2, 2], P[:2, 3], np.ones(2), np.zeros(2), sampling_frequency=fs_hz,
-            Tobs=N / fs_hz, modes=[(2, 2)]).cpu().numpy()
+            Tobs=N / fs_hz, modes=[(2, 2)], return_type="geocenter_td").cpu().numpy()
     for b in range(2):
         hr = c[f"h_{b}"]
         n = int(c["npts"][b])
