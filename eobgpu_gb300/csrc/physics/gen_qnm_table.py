@@ -1,7 +1,9 @@
 """Generate qnm_table.h: fundamental (n = 0) quasi-normal-mode frequencies of
 a Kerr black hole, M omega_lm(a) for (l, m) = (2,2), (2,1), (3,3), (4,4),
-(5,5) and spins -0.99 <= a <= 0.99 on a uniform grid, for the ringdown of
-the waveform (the reference takes them from lalsimulation's tabulated QNMs).
+(5,5) and spins -0.99 <= a <= 0.99, for the ringdown of the waveform (the
+reference takes them from lalsimulation's tabulated QNMs).  The grid is
+uniform in x = sqrt(1 - a): near a = 1 the frequencies go as sqrt(1 - a), so
+they are smooth in x and a four-point interpolation stays accurate there.
 
 Method: Leaver's continued fractions (E. W. Leaver, Proc. R. Soc. Lond. A
 402, 285 (1985)) for gravitational perturbations (s = -2), in units 2M = 1:
@@ -23,7 +25,7 @@ import numpy as np
 
 S = -2
 MODES = [(2, 2), (2, 1), (3, 3), (4, 4), (5, 5)]
-A_MIN, A_MAX, DA = -0.99, 0.99, 0.002
+X_MIN, X_MAX, DX = 0.1, 1.411, 0.001   # x = sqrt(1 - a): a from 0.99 down to -0.990921
 
 
 def _cf(alpha, beta, gamma, n_terms):
@@ -87,42 +89,46 @@ def qnm(l, m, a_spin, w_guess, A_guess):
 SCHWARZSCHILD_GUESS = {2: 0.3737 - 0.0890j, 3: 0.5994 - 0.0927j, 4: 0.8092 - 0.0942j, 5: 1.0123 - 0.0949j}
 
 
-def qnm_at(l, m, a_spin, da=0.05):
-    """M omega of the (l, m, 0) mode at any spin, followed from a = 0 in steps
-    of at most da (no table)."""
+def qnm_at(l, m, a_spin):
+    """M omega of the (l, m, 0) mode at any spin, followed from a = 0 (no
+    table): steps uniform in sqrt(1 - a), 0.01 apart, so that they shrink
+    where the frequencies change fast near a = 1."""
     w, A = qnm(l, m, 0.0, SCHWARZSCHILD_GUESS[l], l * (l + 1) - 2.0)
-    n = int(np.ceil(abs(a_spin) / da))
-    for a in np.linspace(0.0, a_spin, n + 1)[1:]:
-        w, A = qnm(l, m, a, w, A)
+    x1 = np.sqrt(1.0 - a_spin)
+    n = int(np.ceil(abs(x1 - 1.0) / 0.01))
+    for x in np.linspace(1.0, x1, n + 1)[1:]:
+        w, A = qnm(l, m, 1.0 - x * x, w, A)
     return w
 
 
-def table(l, m, grid):
-    """M omega on the grid, followed from a = 0 outwards."""
-    out = np.zeros(len(grid), dtype=complex)
-    i0 = int(np.argmin(np.abs(grid)))
-    w, A = qnm(l, m, grid[i0], SCHWARZSCHILD_GUESS[l], l * (l + 1) - 2.0)
+def table(l, m, spins):
+    """M omega at the given spins, followed from a = 0 outwards."""
+    out = np.zeros(len(spins), dtype=complex)
+    i0 = int(np.argmin(np.abs(spins)))
+    w, A = qnm(l, m, spins[i0], SCHWARZSCHILD_GUESS[l], l * (l + 1) - 2.0)
     out[i0] = w
     for step in (1, -1):
         wp, Ap = w, A
         i = i0 + step
-        while 0 <= i < len(grid):
-            wp, Ap = qnm(l, m, grid[i], wp, Ap)
+        while 0 <= i < len(spins):
+            wp, Ap = qnm(l, m, spins[i], wp, Ap)
             out[i] = wp
             i += step
     return out
 
 
 def main():
-    n = int(round((A_MAX - A_MIN) / DA)) + 1
-    grid = A_MIN + DA * np.arange(n)
-    rows = {lm: table(*lm, grid) for lm in MODES}
+    n = int(round((X_MAX - X_MIN) / DX)) + 1
+    x = X_MIN + DX * np.arange(n)
+    spins = 1.0 - x * x
+    rows = {lm: table(*lm, spins) for lm in MODES}
     w = sys.stdout.write
     w("// Generated by gen_qnm_table.py (Leaver's continued fractions): fundamental Kerr\n")
-    w("// quasi-normal modes M omega_lm(a), e^{-i omega t} convention, on a uniform spin grid.\n")
+    w("// quasi-normal modes M omega_lm(a), e^{-i omega t} convention, on a grid uniform in\n")
+    w("// x = sqrt(1 - a): node j at x = kQnmX0 + j kQnmDx.\n")
     w("#pragma once\n\nnamespace eob {\n\n")
-    w(f"constexpr double kQnmA0 = {A_MIN!r};\nconstexpr double kQnmDa = {DA!r};\nconstexpr int kQnmN = {n};\n")
-    w("// [mode: (2,2), (2,1), (3,3), (4,4), (5,5)][spin][re, im]\n")
+    w(f"constexpr double kQnmX0 = {X_MIN!r};\nconstexpr double kQnmDx = {DX!r};\nconstexpr int kQnmN = {n};\n")
+    w("// [mode: (2,2), (2,1), (3,3), (4,4), (5,5)][node][re, im]\n")
     w(f"constexpr double kQnmTable[5][{n}][2] = {{\n")
     for lm in MODES:
         w("    {\n")

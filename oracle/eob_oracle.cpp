@@ -25,6 +25,7 @@
 #include <algorithm>
 #include "../eobgpu_gb300/csrc/physics/fac_coeffs.h"
 #include "../eobgpu_gb300/csrc/physics/ham_coeffs.h"
+#include "../eobgpu_gb300/csrc/physics/imr_fits.h"
 #include "oracle_dual.h"
 
 using eob::FacCoeffs;
@@ -709,10 +710,9 @@ void oracle_interpolate_td(const double *t, const double *y, double *c1, double 
 // Whole path for one binary: the pieces shared by the free-running and replayed runs.
 namespace {
 
-double post_trajectory(const Binary &b, const Dense &d, int L, double Mt, double dt, int N, const int *ls,
-                       const int *ms, int K, const double *data, double amp, int *npts, double *h_out)
+// multipoles on the trajectory (eob/seobnrv4phm.py:2138-2221): hl[j * L + i]
+std::vector<cplx> modes_on_trajectory(const Binary &b, const Dense &d, int L, const int *ls, const int *ms, int K)
 {
-    // multipoles on the trajectory (eob/seobnrv4phm.py:2138-2221)
     const double nu = b.h.nu;
     std::vector<cplx> hl((size_t)K * L);
     for (int i = 0; i < L; ++i) {
@@ -728,6 +728,13 @@ double post_trajectory(const Binary &b, const Dense &d, int L, double Mt, double
             hl[(size_t)j * L + i] = waveform_mode(b.fc, r, ph, L_, v, Hval, ls[j], ms[j],
                                                   b.a.prefix[eob::lm_index(ls[j], ms[j])], nu, vPhi, 0.0);
     }
+    return hl;
+}
+
+double post_trajectory(const Binary &b, const Dense &d, int L, double Mt, double dt, int N, const int *ls,
+                       const int *ms, int K, const double *data, double amp, int *npts, double *h_out)
+{
+    const std::vector<cplx> hl = modes_on_trajectory(b, d, L, ls, ms, K);
     // synthesis on the uniform grid (eob/seobnrv4phm.py:2310-2372)
     const double Mts = Mt * eob::kMTSUN_SI;
     const double dT = dt / Mts;
@@ -821,6 +828,33 @@ int replay_trajectory(const Binary &b, Dense &d, const double *knots, int L, dou
 
 }  // namespace
 
+namespace {
+// IC (eob/seobnrv4phm.py:1966-2070) and the trajectory, free-running or on
+// given knots; returns the row count (status 1 on failure)
+int trajectory_ex(const double *params, int max_step, double rtol, double atol, double h_init, const double *replay_t,
+                  int replay_L, Binary &b, Dense &d, double *ic, int *status)
+{
+    *status = 0;
+    const double m1 = params[0], m2 = params[1], chi1 = params[2], chi2 = params[3], f0 = params[4];
+    const double Mt = m1 + m2;
+    const double m1s = m1 / Mt, m2s = m2 / Mt;
+    const double omega0 = f0 * (Mt * eob::kMTSUN_SI * PI);
+    build_binary(b, m1s, m2s, chi1, chi2, omega0, 1);
+    const double r_guess = pow(omega0, -2.0 / 3.0);
+    double x[2] = {r_guess, sqrt(r_guess)};
+    root_find_cons(b.h, omega0, x, 1000, 1e-12);
+    const double r0 = x[0], pphi0 = x[1];
+    const double pr0 = root_find_diss(b.h, b.fc, b.a, r0, pphi0, -3e-2, 0.0, 1000, 1e-12, nullptr, 0);
+    if (ic) { ic[0] = r0; ic[1] = pphi0; ic[2] = pr0; }
+    if (replay_t && (replay_L < 2 || replay_L > max_step)) { *status = 1; return 0; }
+    d.t.assign((size_t)max_step, 0.0);
+    d.y.assign((size_t)max_step * 4, 0.0);
+    d.y[0] = r0; d.y[1] = 0.0; d.y[2] = pr0; d.y[3] = pphi0;
+    return replay_t ? replay_trajectory(b, d, replay_t, replay_L, rtol, atol, status)
+                    : free_trajectory(b, d, max_step, rtol, atol, h_init, status);
+}
+}  // namespace
+
 extern "C" {
 
 // Whole path for one binary: IC, trajectory, multipoles, splines, synthesis
@@ -848,32 +882,55 @@ double oracle_lnl_ex(const double *params, double dt, int N, const int *ls, cons
                      const double *data, double amp, double *ic, int *nsteps, double *traj_t, double *traj_y,
                      int *npts, double *h_out, int *status)
 {
-    *status = 0;
-    const double m1 = params[0], m2 = params[1], chi1 = params[2], chi2 = params[3], f0 = params[4];
-    const double Mt = m1 + m2;
-    const double m1s = m1 / Mt, m2s = m2 / Mt;
-    const double omega0 = f0 * (Mt * eob::kMTSUN_SI * PI);
     Binary b;
-    build_binary(b, m1s, m2s, chi1, chi2, omega0, 1);
-    // initial conditions (eob/seobnrv4phm.py:1966-2070)
-    const double r_guess = pow(omega0, -2.0 / 3.0);
-    double x[2] = {r_guess, sqrt(r_guess)};
-    root_find_cons(b.h, omega0, x, 1000, 1e-12);
-    const double r0 = x[0], pphi0 = x[1];
-    const double pr0 = root_find_diss(b.h, b.fc, b.a, r0, pphi0, -3e-2, 0.0, 1000, 1e-12, nullptr, 0);
-    if (ic) { ic[0] = r0; ic[1] = pphi0; ic[2] = pr0; }
-    if (replay_t && (replay_L < 2 || replay_L > max_step)) { *status = 1; return 0.0; }
     Dense d;
-    d.t.assign((size_t)max_step, 0.0);
-    d.y.assign((size_t)max_step * 4, 0.0);
-    d.y[0] = r0; d.y[1] = 0.0; d.y[2] = pr0; d.y[3] = pphi0;
-    const int L = replay_t ? replay_trajectory(b, d, replay_t, replay_L, rtol, atol, status)
-                           : free_trajectory(b, d, max_step, rtol, atol, h_init, status);
+    const int L = trajectory_ex(params, max_step, rtol, atol, h_init, replay_t, replay_L, b, d, ic, status);
     if (nsteps) *nsteps = L;
     if (traj_t) for (int i = 0; i < L; ++i) traj_t[i] = d.t[i];
     if (traj_y) for (int i = 0; i < 4 * L; ++i) traj_y[i] = d.y[i];
     if (L < 2) { *status = 1; return 0.0; }
-    return post_trajectory(b, d, L, Mt, dt, N, ls, ms, K, data, amp, npts, h_out);
+    return post_trajectory(b, d, L, params[0] + params[1], dt, N, ls, ms, K, data, amp, npts, h_out);
+}
+
+// The same run up to the multipoles on the trajectory: rows t[L] [M],
+// y[L][4], modes hl[K][L] (complex, interleaved); returns L
+int oracle_knots_ex(const double *params, const int *ls, const int *ms, int K, int max_step, double rtol, double atol,
+                    double h_init, const double *replay_t, int replay_L, double *traj_t, double *traj_y, double *hl_out,
+                    int *status)
+{
+    Binary b;
+    Dense d;
+    const int L = trajectory_ex(params, max_step, rtol, atol, h_init, replay_t, replay_L, b, d, nullptr, status);
+    if (L < 2) { *status = 1; return L; }
+    for (int i = 0; i < L; ++i) traj_t[i] = d.t[i];
+    for (int i = 0; i < 4 * L; ++i) traj_y[i] = d.y[i];
+    const std::vector<cplx> hl = modes_on_trajectory(b, d, L, ls, ms, K);
+    for (size_t i = 0; i < hl.size(); ++i) { hl_out[2 * i] = hl[i].real(); hl_out[2 * i + 1] = hl[i].imag(); }
+    return L;
+}
+
+// the QNM table lookup of physics/imr_fits.h at spin a: out = (re, im), unit mass
+void oracle_qnm(int l, int m, double a, double *out) { eob::qnm_lookup(l, m, a, &out[0], &out[1]); }
+
+// The fits of the merger-ringdown completion (physics/imr_fits.h) for mode
+// (l, m): out = [delta t_22, |h| peak fit, its first and second derivative,
+// omega, omega dot, c1f, c2f, d1f, d2f, final mass, final spin, QNM re, QNM im
+// (unit remnant mass)]
+void oracle_imr_fits(int l, int m, double m1, double m2, double chi1, double chi2, double *out)
+{
+    const double chiS = 0.5 * (chi1 + chi2), chiA = 0.5 * (chi1 - chi2);
+    const double eta = m1 * m2 / ((m1 + m2) * (m1 + m2));
+    const double chi = chiS + chiA * (m1 - m2) / (m1 + m2) / (1.0 - 2.0 * eta);
+    out[0] = eob::nr_delta_t22(m1, m2, chi1, chi2);
+    out[1] = eob::nr_peak_amp(l, m, m1, m2, chiS, chiA);
+    out[2] = eob::nr_peak_adot(l, m, m1, m2, chiS, chiA);
+    out[3] = eob::nr_peak_addot(l, m, m1, m2, chiS, chiA);
+    out[4] = eob::nr_peak_omega(l, m, eta, chi);
+    out[5] = eob::nr_peak_omegadot(l, m, eta, chi);
+    for (int w = 0; w < 4; ++w) out[6 + w] = eob::rd_coeff(w, l, m, eta, chi);
+    out[10] = eob::final_mass_seobnrv4(m1, m2, chi1, chi2);
+    out[11] = eob::final_spin_hbr2016(m1, m2, chi1, chi2);
+    eob::qnm_lookup(l, m, out[11], &out[12], &out[13]);
 }
 
 double oracle_lnl_one(const double *params, double dt, int N, const int *ls, const int *ms, int K, int max_step,

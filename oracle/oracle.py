@@ -23,7 +23,9 @@ def build(force: bool = False) -> str:
     src = os.path.join(HERE, "eob_oracle.cpp")
     deps = [src, os.path.join(HERE, "oracle_dual.h"),
             os.path.join(HERE, "..", "eobgpu_gb300", "csrc", "physics", "fac_coeffs.h"),
-            os.path.join(HERE, "..", "eobgpu_gb300", "csrc", "physics", "ham_coeffs.h")]
+            os.path.join(HERE, "..", "eobgpu_gb300", "csrc", "physics", "ham_coeffs.h"),
+            os.path.join(HERE, "..", "eobgpu_gb300", "csrc", "physics", "imr_fits.h"),
+            os.path.join(HERE, "..", "eobgpu_gb300", "csrc", "physics", "qnm_table.h")]
     if not force and os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(d) for d in deps):
         return LIB_PATH
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
