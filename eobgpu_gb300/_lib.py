@@ -22,7 +22,7 @@ class EobOptions(ctypes.Structure):
     _fields_ = [("rtol", c_double), ("atol", c_double), ("h_init", c_double), ("step_back", c_double),
                 ("fine_step", c_double), ("ic_mode", c_int), ("precision", c_int), ("block", c_int),
                 ("grid", c_int), ("max_tries", c_ll), ("lanes_per_binary", c_int), ("spline_tile", c_int),
-                ("head_quads", c_int)]
+                ("head_quads", c_int), ("imr", c_int)]
 
 
 class EobViews(ctypes.Structure):
@@ -37,6 +37,7 @@ _P = c_void_p
 _SIGS = {
     "eob_options_default": (None, [ctypes.POINTER(EobOptions)]),
     "eob_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int]),
+    "eob_workspace_bytes_imr": (c_size_t, [c_int, c_int, c_int, c_int]),
     "eob_waveform_lnl": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, _P, _P, c_int, _P, _P, c_int, c_double,
                                  _P, c_int, c_double, ctypes.POINTER(EobOptions), _P, _P, _P]),
     "eob_waveform_strain": (c_int, [_P, c_size_t, c_int, c_int, c_int, c_int, _P, _P, c_int, _P, _P, c_int,

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libeobgb300.so")
-SOURCES = ["k_setup.cu", "k_integrate.cu", "k_post.cu", "k_compat.cu", "k_tdinterp.cu", "k_fd.cu", "k_hooks.cu", "k_noalloc.cu",
+SOURCES = ["k_setup.cu", "k_integrate.cu", "k_post.cu", "k_imr.cu", "k_compat.cu", "k_tdinterp.cu", "k_fd.cu", "k_hooks.cu", "k_noalloc.cu",
            "eob_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC]

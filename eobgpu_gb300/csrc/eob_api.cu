@@ -23,6 +23,7 @@ void eob_options_default(eob_options *o)
     o->lanes_per_binary = 0;
     o->spline_tile = 0;
     o->head_quads = -1;
+    o->imr = 0;
 }
 
 size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples)
@@ -31,11 +32,21 @@ size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_
     return ws_layout(max_batch, max_steps, max_modes, max_samples).total;
 }
 
+size_t eob_workspace_bytes_imr(int max_batch, int max_steps, int max_modes, int max_samples)
+{
+    if (max_batch < 1 || max_steps < 4 || max_modes < 1 || max_modes > kMaxModes || max_samples < 1) return 0;
+    return ws_layout(max_batch, max_steps, max_modes, max_samples, 1).total;
+}
+
+// the workspace's layout: with the merger-ringdown section when it is large enough for one
 static bool dims_ok(size_t workspace_bytes, int max_batch, int max_steps, int max_modes, int max_samples, WsLayout *L)
 {
-    *L = ws_layout(max_batch, max_steps, max_modes, max_samples);
-    return max_batch >= 1 && max_steps >= 4 && max_modes >= 1 && max_modes <= kMaxModes && max_samples >= 1 &&
-           workspace_bytes >= L->total;
+    if (!(max_batch >= 1 && max_steps >= 4 && max_modes >= 1 && max_modes <= kMaxModes && max_samples >= 1))
+        return false;
+    *L = ws_layout(max_batch, max_steps, max_modes, max_samples, 1);
+    if (workspace_bytes >= L->total) return true;
+    *L = ws_layout(max_batch, max_steps, max_modes, max_samples, 0);
+    return workspace_bytes >= L->total;
 }
 
 static bool modes_ok(const int *ells, const int *mms, int K, int max_modes)
@@ -63,11 +74,13 @@ int eob_prepare_stages(void *workspace, size_t workspace_bytes, int max_batch, i
     for (int j = 0; j < K; ++j) { a.ells[j] = ells[j]; a.mms[j] = mms[j]; }
     a.dt = dt;
     if (opt) a.opt = *opt; else eob_options_default(&a.opt);
+    if (a.opt.imr && !L.imr) return EOB_E_ARG;  // the workspace has no merger-ringdown section
     const Ws w = ws_views(workspace, L);
     cudaError_t e = cudaSuccess;
     if (stages & 1) e = launch_setup(w, a, stream);
     if (e == cudaSuccess && (stages & 2)) e = launch_integrate(w, a, stream);
     if (e == cudaSuccess && (stages & 4)) e = launch_prepare_post(w, a, stream);
+    if (e == cudaSuccess && (stages & 4)) e = launch_imr(w, a, stream);
     return e == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 

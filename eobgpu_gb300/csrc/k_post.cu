@@ -148,6 +148,7 @@ __device__ __forceinline__ int find_segment(const long long *off, int B, long lo
 struct ModeArgs {
     int K;
     int ells[kMaxModes], mms[kMaxModes];
+    int imr;  // also r and p_r as series for the merger-ringdown attachment
 };
 
 __global__ void __launch_bounds__(128) k_modes(Ws w, int B, ModeArgs ma)
@@ -162,6 +163,10 @@ __global__ void __launch_bounds__(128) k_modes(Ws w, int B, ModeArgs ma)
         const double rr = row[1], phi = row[2], pr = row[3], pphi = row[4];
         w.tin[r] = t_in_of(row[0], rec.Mt);
         w.ys[r] = phi;
+        if (ma.imr) {
+            w.imr_ys[r] = rr;
+            w.imr_ys[Rc + r] = pr;
+        }
         HamEval e;
         ham_eval(rec.ham, rr, pr, pphi, &e);
         const double v = cbrt(e.dHdL);
@@ -254,7 +259,7 @@ constexpr int kSplineMaxTile = 8;      // series (warps) per block
 // block boundaries (gathered by shuffles), and every lane back-substitutes
 // its rows; the cubic coefficients are then computed lane-strided.  Scratch:
 // the series' own coefficient rows (ld/dg/ud/Bv = c3/c2/c1/rhs arrays).
-__global__ void __launch_bounds__(32 * kSplineMaxTile) k_spline(Ws w, int B, int nsubs, int mixed)
+__global__ void __launch_bounds__(32 * kSplineMaxTile) k_spline(Ws w, int B, int nsubs, int nmain, int mixed)
 {
     __shared__ double s_z[kSplineMaxTile][2][32];   // boundary solution: u_j = x_{e_j}, t_{j+1} = x_{s_{j+1}}
     __shared__ double s_f[kSplineMaxTile][5][32];   // reduced elimination per interface: d01, d10, f0, f1, ws_{j+1}
@@ -267,9 +272,13 @@ __global__ void __launch_bounds__(32 * kSplineMaxTile) k_spline(Ws w, int B, int
     const int n = w.nsteps[b];
     const size_t Rc = (size_t)w.L.Bc * (size_t)w.L.Lc;
     const size_t base = (size_t)w.row_off[b];
-    const size_t o = (size_t)sub * Rc + base;
-    const double *x = w.tin + base, *y = w.ys + o;
-    double *Bv = w.cD + o, *ud = w.cA + o, *dg = w.cB + o, *ld = w.cC + o;
+    // series 0 .. nmain - 1: phase and modes; nmain, nmain + 1: r and p_r of the
+    // merger-ringdown section
+    const bool extra = sub >= nmain;
+    const size_t o = (size_t)(extra ? sub - nmain : sub) * Rc + base;
+    const double *x = w.tin + base, *y = (extra ? w.imr_ys : w.ys) + o;
+    double *Bv = (extra ? w.imr_cD : w.cD) + o, *ud = (extra ? w.imr_cA : w.cA) + o,
+           *dg = (extra ? w.imr_cB : w.cB) + o, *ld = (extra ? w.imr_cC : w.cC) + o;
 
     for (int i = lane; i < n; i += 32) spline_row(x, y, n, i, &ld[i], &dg[i], &ud[i], &Bv[i]);
     __syncwarp();
@@ -393,7 +402,7 @@ __global__ void __launch_bounds__(32 * kSplineMaxTile) k_spline(Ws w, int B, int
         dg[i] = (slope - bi) / dx - t;
         ld[i] = t / dx;
     }
-    if (mixed && sub >= 1) {
+    if (mixed && sub >= 1 && sub < nmain) {
         __syncwarp();
         // FP32 copies of the amplitude series for the mixed-precision synthesis
         const size_t S = (size_t)2 * w.L.Kc * Rc;
@@ -432,6 +441,19 @@ __device__ __forceinline__ int knot_index(const double *x, int n, double t)
     return i;
 }
 
+// the merger-ringdown of one mode x = t - t_match after the match point
+// (compute_MR_mode_free, eob/seobnrv4phm.py:1830-1843)
+__device__ __forceinline__ void ringdown_mode(const ImrRec &c, double x, double *hr, double *hi)
+{
+    const double A = c.c1c * tanh(c.c1f * x + c.c2f) + c.c2c;
+    const double ph = c.phi_match - c.d1c * log((1 + c.d2f * exp(-c.d1f * x)) / (1 + c.d2f)) - c.om_re * x;
+    const double mag = c.eta * A * exp(-c.om_im * x);
+    double sp, cp;
+    sincos(ph, &sp, &cp);
+    *hr = mag * cp;
+    *hi = mag * sp;
+}
+
 __global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
 {
     __shared__ double s_red[256 / 32];
@@ -441,6 +463,10 @@ __global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
         const int b = find_segment(w.chunk_off, sa.B, c);
         const int j = (int)(c - w.chunk_off[b]);
         const int np = w.npts[b];
+        // with the merger-ringdown: samples 0 .. idx are the NQC-corrected
+        // inspiral, idx + 1 .. np - 1 the ringdown, zero beyond (per mode too)
+        const bool imr = w.imr_bin && w.imr_bin[b].on;
+        const int idx = imr ? w.imr_bin[b].idx : np;
         const int nuse = (sa.mode == 2) ? sa.N : (np < sa.N ? np : sa.N);
         const int n = w.nsteps[b];
         const size_t base = (size_t)w.row_off[b];
@@ -448,17 +474,55 @@ __global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
         const double Mts = w.bins[b].Mt * kMTSUN_SI;
         const double dT = sa.dt / Mts;
         const double t0 = x[0], tend = x[n - 1];
+        const ImrRec *recs = imr ? w.imr_rec + (size_t)b * w.L.Kc : nullptr;
         double acc = 0.0;
         const int kbeg = j * kChunk;
         const int kend = min(nuse, kbeg + kChunk);
         for (int k = kbeg + threadIdx.x; k < kend; k += blockDim.x) {
+            double hsum = 0.0, hsum_i = 0.0;
+            if (imr && k > idx) {
+                if (k < np) {
+                    const double xr = (k - idx) * dT;
+                    for (int q = 0; q < sa.K; ++q) {
+                        double hr, hi;
+                        ringdown_mode(recs[q], xr, &hr, &hi);
+                        if (sa.mode == 2) {
+                            const size_t oo = 2 * (((size_t)b * sa.K + q) * (size_t)sa.N + k);
+                            sa.out[oo] = hr;
+                            sa.out[oo + 1] = hi;
+                        }
+                        hsum += hr;
+                        hsum_i += hi;
+                    }
+                } else if (sa.mode == 2) {
+                    for (int q = 0; q < sa.K; ++q) {
+                        const size_t oo = 2 * (((size_t)b * sa.K + q) * (size_t)sa.N + k);
+                        sa.out[oo] = 0.0;
+                        sa.out[oo + 1] = 0.0;
+                    }
+                }
+                if (sa.mode == 1) {
+                    sa.out[2 * ((size_t)b * sa.N + k)] = hsum;
+                    sa.out[2 * ((size_t)b * sa.N + k) + 1] = hsum_i;
+                } else if (sa.mode == 0) {
+                    const double hk = sa.amp * hsum;
+                    acc += hk * hk - 2.0 * sa.data[k] * hk;
+                }
+                continue;
+            }
             double t = k * dT + t0;
             if (t > tend) t = tend;
             const int i = knot_index(x, n, t);
             const double xx = t - x[i], x2 = xx * xx, x3 = x2 * xx;
             const size_t o = base + i;
             const double phi = w.ys[o] + w.cA[o] * xx + w.cB[o] * x2 + w.cC[o] * x3;
-            double hsum = 0.0, hsum_i = 0.0;
+            double rr = 0.0, pr = 0.0, om = 0.0;
+            if (imr) {
+                om = w.cA[o] + 2 * w.cB[o] * xx + 3 * w.cC[o] * x2;
+                rr = w.imr_ys[o] + w.imr_cA[o] * xx + w.imr_cB[o] * x2 + w.imr_cC[o] * x3;
+                const size_t op = Rc + o;
+                pr = w.imr_ys[op] + w.imr_cA[op] * xx + w.imr_cB[op] * x2 + w.imr_cC[op] * x3;
+            }
             for (int q = 0; q < sa.K; ++q) {
                 const size_t orr = (size_t)(1 + 2 * q) * Rc + o, oi = (size_t)(2 + 2 * q) * Rc + o;
                 const double re = w.ys[orr] + w.cA[orr] * xx + w.cB[orr] * x2 + w.cC[orr] * x3;
@@ -466,7 +530,19 @@ __global__ void __launch_bounds__(256) k_synth(Ws w, SynthArgs sa)
                 double sp, cp;
                 sincos(sa.mms[q] * phi, &sp, &cp);
                 // (re + i im) e^{-i m phi}
-                const double hr = re * cp + im * sp, hi = im * cp - re * sp;
+                double hr = re * cp + im * sp, hi = im * cp - re * sp;
+                if (imr) {
+                    // NQC correction (EOBNonQCCorrection, eob/seobnrv4phm.py:1686-1700)
+                    const ImrRec &cq = recs[q];
+                    const double sr = sqrt(rr), rO = rr * om;
+                    const double mag = 1.0 + (pr * pr / (rO * rO)) * (cq.a1 + cq.a2 / rr + cq.a3 / (rr * sr));
+                    const double nph = cq.b1 * pr / rO + pr * pr * pr / rO * cq.b2;
+                    double ns, nc;
+                    sincos(nph, &ns, &nc);
+                    const double tr = mag * (hr * nc - hi * ns);
+                    hi = mag * (hr * ns + hi * nc);
+                    hr = tr;
+                }
                 if (sa.mode == 2) {
                     const size_t oo = 2 * (((size_t)b * sa.K + q) * (size_t)sa.N + k);
                     sa.out[oo] = hr;
@@ -516,6 +592,8 @@ __global__ void __launch_bounds__(256) k_synth_mixed(Ws w, SynthArgs sa)
         const int j = (int)(c - w.chunk_off[b]);
         const int np = w.npts[b];
         const int nuse = np < sa.N ? np : sa.N;
+        // the merger-ringdown runs in the FP64 synthesis only
+        const bool imr_bin = w.imr_bin && w.imr_bin[b].on;
         const int n = w.nsteps[b];
         const size_t base = (size_t)w.row_off[b];
         const double *x = w.tin + base;
@@ -567,7 +645,7 @@ __global__ void __launch_bounds__(256) k_synth_mixed(Ws w, SynthArgs sa)
         if (threadIdx.x == 0 && sa.mode == 0) {
             double sum = 0.0;
             for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += s_red[q];
-            w.partial[c] = have_f32 ? sum : __longlong_as_double(0x7ff8000000000000ll);
+            w.partial[c] = (have_f32 && !imr_bin) ? sum : __longlong_as_double(0x7ff8000000000000ll);
         }
         __syncthreads();
     }
@@ -595,11 +673,14 @@ cudaError_t launch_prepare_post(const Ws &w, const RunArgs &a, cudaStream_t s)
     ModeArgs ma;
     ma.K = a.K;
     for (int j = 0; j < kMaxModes; ++j) { ma.ells[j] = a.ells[j]; ma.mms[j] = a.mms[j]; }
+    ma.imr = (a.opt.imr && w.imr_ys) ? 1 : 0;
     k_modes<<<nsm * 8, 128, 0, s>>>(w, a.B, ma);
-    const int nsubs = 1 + 2 * a.K;
+    const int nmain = 1 + 2 * a.K;
+    const int nsubs = nmain + (ma.imr ? 2 : 0);
     const int tile = (a.opt.spline_tile >= 1 && a.opt.spline_tile <= kSplineMaxTile) ? a.opt.spline_tile : 4;
     const long long series = (long long)a.B * nsubs;
-    k_spline<<<(unsigned)((series + tile - 1) / tile), 32 * tile, 0, s>>>(w, a.B, nsubs, a.opt.precision == 1 ? 1 : 0);
+    k_spline<<<(unsigned)((series + tile - 1) / tile), 32 * tile, 0, s>>>(w, a.B, nsubs, nmain,
+                                                                         a.opt.precision == 1 ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -608,7 +689,7 @@ cudaError_t launch_synth(const Ws &w, const RunArgs &a, int mode, double *out, c
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int mixed = (mode != 2 && a.opt.precision == 1) ? 1 : 0;
+    const int mixed = (mode != 2 && a.opt.precision == 1 && !a.opt.imr) ? 1 : 0;
     k_scan_chunks<<<1, kScanThreads, 0, s>>>(w, a.B, a.N, mode == 2 ? 1 : 0, mode == 0 ? a.data : nullptr,
                                              mode == 0 ? mixed : 0);
     if (mode == 1) {

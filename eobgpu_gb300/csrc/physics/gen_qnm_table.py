@@ -123,20 +123,21 @@ def main():
     spins = 1.0 - x * x
     rows = {lm: table(*lm, spins) for lm in MODES}
     w = sys.stdout.write
-    w("// Generated by gen_qnm_table.py (Leaver's continued fractions): fundamental Kerr\n")
-    w("// quasi-normal modes M omega_lm(a), e^{-i omega t} convention, on a grid uniform in\n")
+    w("// Generated by gen_qnm_table.py (Leaver's continued fractions); do not edit.  Fundamental\n")
+    w("// Kerr quasi-normal modes M omega_lm(a), e^{-i omega t} convention, on a grid uniform in\n")
     w("// x = sqrt(1 - a): node j at x = kQnmX0 + j kQnmDx.\n")
     w("#pragma once\n\nnamespace eob {\n\n")
-    w(f"constexpr double kQnmX0 = {X_MIN!r};\nconstexpr double kQnmDx = {DX!r};\nconstexpr int kQnmN = {n};\n")
+    w(f"constexpr double kQnmX0 = {X_MIN!r};\nconstexpr double kQnmDx = {DX!r};\nconstexpr int kQnmN = {n};\n\n")
+    w("}  // namespace eob\n\n")
     w("// [mode: (2,2), (2,1), (3,3), (4,4), (5,5)][node][re, im]\n")
-    w(f"constexpr double kQnmTable[5][{n}][2] = {{\n")
+    w("#define EOB_QNM_INIT \\\n    { \\\n")
     for lm in MODES:
-        w("    {\n")
+        w("        { \\\n")
         vals = rows[lm]
         for j in range(0, n, 2):
-            w("        " + " ".join(f"{{{v.real.hex()}, {v.imag.hex()}}}," for v in vals[j:j + 2]) + "\n")
-        w("    },\n")
-    w("};\n\n}  // namespace eob\n")
+            w("            " + " ".join(f"{{{v.real.hex()}, {v.imag.hex()}}}," for v in vals[j:j + 2]) + " \\\n")
+        w("        }, \\\n")
+    w("    }\n")
 
 
 if __name__ == "__main__":

