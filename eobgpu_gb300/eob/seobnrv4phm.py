@@ -270,11 +270,15 @@ def fd_likelihood(hp_fd, hc_fd, data, psd, Fplus, Fcross, time_shift, df, num_bi
 
 
 class SEOBNRv4PHM:
-    """Aligned-spin SEOBNR waveform generator (eob/seobnrv4phm.py:1845-2726)."""
+    """Aligned-spin SEOBNR waveform generator (eob/seobnrv4phm.py:1845-2726).
+
+    imr (default True, as the reference's __call__): the modes carry the NQC
+    correction and the merger-ringdown (compute_full_waveform, :2374-2557);
+    imr=False stops at the trajectory's end."""
 
     allowable_modes_hlms = [(2, 2), (2, 1), (3, 3), (4, 4), (5, 5)]
 
-    def __init__(self, max_init_len=-1, use_gpu=True, ell_max=8, max_step=20000, options=None, **kwargs):
+    def __init__(self, max_init_len=-1, use_gpu=True, ell_max=8, max_step=20000, options=None, imr=True, **kwargs):
         if max_init_len > 0:
             raise NotImplementedError
         self.use_gpu = True
@@ -286,7 +290,8 @@ class SEOBNRv4PHM:
         self.ells_default = np.array([l for l, _ in self.allowable_modes_hlms], dtype=np.int32)
         self.mms_default = np.array([m for _, m in self.allowable_modes_hlms], dtype=np.int32)
         self.max_step = max_step
-        self.options = options
+        self.options = _lib.default_options() if options is None else _lib.EobOptions.from_buffer_copy(options)
+        self.options.imr = 1 if imr else 0
         self.eob_c_class = pyEOB.SEOBNRv5Class()
         self.integrator = DOPR853(self.eob_c_class, stopping_criterion=StoppingCriterion(self.eob_c_class, max_step),
                                   tmax=1e7 * 1e6, max_step=max_step)

@@ -18,7 +18,7 @@ def test_waveform_call_modes(torch_cuda, golden):
     from eob.seobnrv4phm import SEOBNRv4PHM
     c = golden["config1"]
     P = c["params"]
-    gen = SEOBNRv4PHM(use_gpu=True, max_step=4096)
+    gen = SEOBNRv4PHM(use_gpu=True, max_step=4096, imr=False)
     out = gen(P[:, 0], P[:, 1], P[:, 2], P[:, 3], np.ones(len(P)), np.zeros(len(P)), modes=[(2, 2)], fs=20.0,
               sampling_frequency=1.0 / float(c["dt"]))
     out = out.cpu().numpy()
@@ -41,7 +41,7 @@ def test_step_by_step_initial_conditions_and_trajectory(torch_cuda, golden):
     from eob.seobnrv4phm import SEOBNRv4PHM, MTSUN_SI
     c = golden["config1"]
     P = c["params"][:3]
-    gen = SEOBNRv4PHM(use_gpu=True, max_step=4096)
+    gen = SEOBNRv4PHM(use_gpu=True, max_step=4096, imr=False)
     mt = P[:, 0] + P[:, 1]
     omega0 = 20.0 * (mt * MTSUN_SI * np.pi)
     gen.setup_class(P[:, 0] / mt, P[:, 1] / mt, P[:, 2], P[:, 3], omega0)
@@ -59,7 +59,7 @@ def test_bbh_td_strain_and_likelihood(torch_cuda, golden):
     P = c["params"]
     fs_hz = 1.0 / float(c["dt"])
     N = int(c["N"])
-    bbh = BBHWaveformTD(None, amp_phase_kwargs={"max_step": 4096})
+    bbh = BBHWaveformTD(None, amp_phase_kwargs={"max_step": 4096, "imr": False})
     h = bbh(P[:2, 0], P[:2, 1], P[:2, 2], P[:2, 3], np.ones(2), np.zeros(2), sampling_frequency=fs_hz,
             Tobs=N / fs_hz, modes=[(2, 2)], return_type="geocenter_td").cpu().numpy()
     for b in range(2):

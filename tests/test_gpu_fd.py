@@ -87,7 +87,8 @@ def bbh(torch_cuda):
     asd = np.full(Nf, 1.0)
     asd[:10] = np.inf
     ifos = [Interferometer(D[c], V[c], asd, np.zeros(Nf, complex)) for c in range(3)]
-    gen = BBHWaveformTD(ifos)
+    # inspiral-only templates: the oracle comparison below replays the inspiral
+    gen = BBHWaveformTD(ifos, amp_phase_kwargs={"imr": False})
     cfg = workload.CONFIGS[1]
     P = workload.draw_params(cfg)
     B = len(P)
@@ -105,7 +106,7 @@ def bbh(torch_cuda):
     data = (Fp[:, 0, None] * hp + Fx[:, 0, None] * hc) * np.exp(-2j * np.pi * f * tau[:, 0, None])
     data += 0.3 * (rng.standard_normal((3, Nf)) + 1j * rng.standard_normal((3, Nf)))
     ifos = [Interferometer(D[c], V[c], asd, data[c]) for c in range(3)]
-    gen = BBHWaveformTD(ifos)
+    gen = BBHWaveformTD(ifos, amp_phase_kwargs={"imr": False})
     return gen, params, fs, Tobs, D, V, data, asd
 
 

@@ -70,10 +70,24 @@ def test_imr_vs_oracle_on_gpu_knots(runs, oracle, K):
     print(f"\nIMR K={K}: summed strain {worst[0]:.2e}, worst mode {worst[1]:.2e} of peak, lnL {worst[2]:.2e}")
 
 
-def test_imr_changes_only_the_end(runs):
-    """The inspiral before the attachment is the inspiral-only waveform
-    times the NQC factor (|factor - 1| small far from merger): the two
-    templates agree closely early on and differ at the merger."""
-    c, out = runs
-    lnl, st, npts, trajs, hm, hs = out[1]
-    assert np.all(npts > 0)
+def test_mirror_waveform_class_attaches_the_ringdown(golden, oracle):
+    """The drop-in SEOBNRv4PHM (imr on by default, as the reference's
+    __call__) returns per-mode IMR waveforms: against the oracle's IMR on the
+    generator's own knots, every mode within 1e-8 of its peak, divided by the
+    distance."""
+    from eobgpu_gb300.eob.seobnrv4phm import SEOBNRv4PHM
+    from oracle import imr_oracle as imr
+    c = golden["config1"]
+    P = c["params"][:3]
+    dist = np.array([1.0, 2.0, 4.0])
+    gen = SEOBNRv4PHM(max_step=4096)
+    fs = 1.0 / float(c["dt"])
+    out = gen(P[:, 0], P[:, 1], P[:, 2], P[:, 3], dist, np.zeros(3), fs=20.0, sampling_frequency=fs).cpu().numpy()
+    _, _, _, trajs = gen._wl.trajectories()
+    for b in range(3):
+        md, info = imr.waveform(oracle, P[b], float(c["dt"]), MODES5, replay_t=trajs[b][0])
+        n = int(info["npts_imr"])
+        for q in range(5):
+            ref = md[q] / dist[b]
+            assert np.max(np.abs(out[b, q, :n] - ref)) < 1e-8 * np.max(np.abs(ref)), (b, q)
+            assert np.all(out[b, q, n:] == 0)
