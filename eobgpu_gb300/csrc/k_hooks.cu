@@ -23,14 +23,14 @@ __global__ void k_fp64_probe(double *out, int iters)
     out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
-// out[8 i + 0..7] = eob_rcp, 1/x, eob_rcbrt, rcbrt, eob_log, log, eob_rsqrt,
-// eob_inv_eighth_root of x[i].
+// out[10 i + 0..9] = eob_rcp, 1/x, eob_rcbrt, rcbrt, eob_log, log, eob_rsqrt,
+// eob_inv_eighth_root, eob_expm1_neg (of min(x, 600)), expm1(-min(x, 600)) of x[i].
 __global__ void k_math_probe(const double *x, int n, double *out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double v = x[i];
-    double *o = out + 8 * (size_t)i;
+    double *o = out + 10 * (size_t)i;
     o[0] = eob::eob_rcp(v);
     o[1] = 1.0 / v;
     o[2] = eob::eob_rcbrt(v);
@@ -39,6 +39,9 @@ __global__ void k_math_probe(const double *x, int n, double *out)
     o[5] = log(v);
     o[6] = eob::eob_rsqrt(v);
     o[7] = eob::eob_inv_eighth_root(v);
+    const double y = v < 600.0 ? v : 600.0;
+    o[8] = eob::eob_expm1_neg(y);
+    o[9] = expm1(-y);
 }
 
 constexpr int kHookThreads = 256;  // 8 warps: 4 pairs or 2 four-warp groups per block

@@ -214,6 +214,8 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     const unsigned gmask = (GW == 32) ? 0xffffffffu : (((1u << GW) - 1u) << (lane - sub));
     X *xch = nullptr;
     PairSync ps{0u, 0u, true};
+    QuadLane ql{};
+    if constexpr (G == 128) ql = quad_lane(role, lane);
     if constexpr (kPair) {
         const int grp = (int)(threadIdx.x / G);
         xch = &xch_all[grp];
@@ -353,7 +355,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
         double kk[4];
         if constexpr (G == 1) eob_rhs(rec->ham, rec->flux, arg, kk);
         else if constexpr (G == 64) eob_rhs_pair(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
-        else if constexpr (G == 128) eob_rhs_quad(rec->jets, rec->flux, arg, kk, lane, role, *xch, ps);
+        else if constexpr (G == 128) eob_rhs_quad(rec->jets, rec->flux, ql, arg, kk, lane, role, *xch, ps);
         else eob_rhs_group<G>(rec->jets, rec->flux, arg, kk, sub);
         if constexpr (kPair) {
             if (!ps.ok) {

@@ -454,13 +454,25 @@ EOB_HD FluxLane flux_lane_make(const FluxTable &t, double pphi, double omega, do
     return flux_lane_make_lv(t, pphi, omega, Hreal, v, w, eob_log(v));
 }
 
-// m x / (1 - e^{-m x}) and 4 k^2 = 4 (m H omega)^2 for one m
+// m x / (1 - e^{-m x}) and 4 k^2 = 4 (m H omega)^2 for one m (md = m as a
+// double); 1 - e^{-m x} from eob_expm1_neg, without the cancellation of
+// 1 - exp(-m x) at small m x
+EOB_HD double flux_m_factor_T(double md, double x)
+{
+    const double xm = md * x;
+    return xm * eob_rcp(-eob_expm1_neg(xm));
+}
+
+EOB_HD double flux_m_factor_k4(double md, double hw)
+{
+    const double km = md * hw;
+    return 4.0 * km * km;
+}
+
 EOB_HD void flux_m_factors(int m, double x, double hw, double *T, double *k4)
 {
-    const double xm = m * x;
-    *T = xm * eob_rcp(1.0 - exp(-xm));
-    const double km = m * hw;
-    *k4 = 4.0 * km * km;
+    *T = flux_m_factor_T((double)m, x);
+    *k4 = flux_m_factor_k4((double)m, hw);
 }
 
 // l and m of lm_index i, packed (l << 4) | m
@@ -490,9 +502,20 @@ EOB_HD int lm_packed(int i)
 // the series part without the v_phi power: S^2 (rho_lm^l + f_lm)^2
 // the series part from rho_lm's sum: S^2 (rho_lm^l + f_lm)^2 with the h22
 // calibration term
-EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, double rho)
+// a flag of the table (0.0 or 1.0) as a bool; on the device by its bits (a
+// comparison of doubles takes an FP64 issue slot)
+EOB_HD bool table_flag(double x)
 {
-    const int lm = lm_packed(i);
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(x) != 0;
+#else
+    return x != 0.0;
+#endif
+}
+
+// lm: lm_packed(i), passed by callers that keep it in a register
+EOB_HD double flux_mode_s_rho_lm(const FluxTable &t, int i, int lm, const FluxLane &f, double rho)
+{
     const int l = lm >> 4, m = lm & 15;
     const int eps = (l + m) & 1;
     rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
@@ -503,15 +526,20 @@ EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, doub
     if (l & 1) rpl *= rho;
     if (l == 8) rpl = r4 * r4;
     const double aux = f.v * fma(t.f3[i], f.v2, t.f1[i]);
-    rpl = ((m & 1) && t.equal_mass != 0.0) ? aux : rpl + aux;
+    rpl = ((m & 1) && table_flag(t.equal_mass)) ? aux : rpl + aux;
     const double S2 = eps ? f.S2o : f.S2e;
     return S2 * (rpl * rpl);
 }
 
-template <int KMAX>
-EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
+EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, double rho)
 {
-    const int m = lm_packed(i) & 15;
+    return flux_mode_s_rho_lm(t, i, lm_packed(i), f, rho);
+}
+
+template <int KMAX>
+EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &f)
+{
+    const int m = lm & 15;
     const double elm = t.elog[m] + f.lv;
     // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
     double acc = t.rho[i][KMAX];
@@ -522,22 +550,32 @@ EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
         if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
         acc = fma(acc, f.v, ck);
     }
-    return flux_mode_s_rho(t, i, f, fma(acc, f.v, 1.0));
+    return flux_mode_s_rho_lm(t, i, lm, f, fma(acc, f.v, 1.0));
+}
+
+template <int KMAX>
+EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
+{
+    return flux_mode_s_lm<KMAX>(t, i, lm_packed(i), f);
 }
 
 // rho_lm's series (degree <= 10) in two halves for two lanes: half 0 gives
 // c_1 + c_2 v + ... + c_5 v^4 and half 1 gives c_6 + c_7 v + ... + c_10 v^4,
 // c_k = rho_k + rhol_k eulerlog_m (rhol_k is zero where the series has no
 // log term); then rho = 1 + v (half 0 + v^5 half 1)
-EOB_HD double flux_rho_half(const FluxTable &t, int i, const FluxLane &f, int half)
+EOB_HD double flux_rho_half_m(const FluxTable &t, int i, int m, const FluxLane &f, int half)
 {
-    const int m = lm_packed(i) & 15;
     const double elm = t.elog[m] + f.lv;
     const double *rh = t.rho[i] + (half ? 6 : 1), *rl = t.rhol[i] + (half ? 6 : 1);
     double acc = fma(rl[4], elm, rh[4]);
 #pragma unroll
     for (int k = 3; k >= 0; --k) acc = fma(acc, f.v, fma(rl[k], elm, rh[k]));
     return acc;
+}
+
+EOB_HD double flux_rho_half(const FluxTable &t, int i, const FluxLane &f, int half)
+{
+    return flux_rho_half_m(t, i, lm_packed(i) & 15, f, half);
 }
 
 // vphi^(2 (l + eps)) of multipole i selected from the precomputed powers
@@ -559,9 +597,8 @@ EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
 }
 
 // vphi^(2 (l + eps)) of multipole i from vphi^2 by squaring (l + eps = 2..9)
-EOB_HD double flux_mode_vp_sq(int i, double vphi2)
+EOB_HD double flux_mode_vp_sq_lm(int lm, double vphi2)
 {
-    const int lm = lm_packed(i);
     const int e = (lm >> 4) + (((lm >> 4) + (lm & 15)) & 1);
     const double p2 = vphi2 * vphi2, p4 = p2 * p2;
     double r = (e & 1) ? vphi2 : 1.0;
@@ -571,18 +608,25 @@ EOB_HD double flux_mode_vp_sq(int i, double vphi2)
     return r;
 }
 
+EOB_HD double flux_mode_vp_sq(int i, double vphi2) { return flux_mode_vp_sq_lm(lm_packed(i), vphi2); }
+
 // LD: an upper bound on l of the multipoles evaluated together (the table's
 // coefficients above l are zero)
 template <int LD = kLMax>
-EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
+EOB_HD double flux_mode_b_l(const FluxTable &t, int i, int l, double T, double k4)
 {
-    const int l = lm_packed(i) >> 4;
     // prod_{j<=l} (4 k^2 + j^2)
     const double *c = tprod_row(l);
     double P = c[LD];
 #pragma unroll
     for (int q = LD - 1; q >= 0; --q) P = fma(P, k4, c[q]);
     return t.gmul[i] * T * P;
+}
+
+template <int LD = kLMax>
+EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
+{
+    return flux_mode_b_l<LD>(t, i, lm_packed(i) >> 4, T, k4);
 }
 
 template <int KMAX, int LD = kLMax>

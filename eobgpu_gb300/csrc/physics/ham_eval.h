@@ -13,36 +13,63 @@
 
 namespace eob {
 
-// 1/sqrt(x): the device's reciprocal square root (one instruction sequence
-// instead of a square root and a division); on the host 1/sqrt(x)
-EOB_HD double eob_rsqrt(double x)
-{
 #ifdef __CUDA_ARCH__
-    return rsqrt(x);
-#else
-    return 1.0 / sqrt(x);
-#endif
+// Conversions between double and float by integer operations.  On GB300 a
+// conversion instruction (F64 <-> F32) has the latency of a DFMA (about 65
+// cycles); these take a few integer instructions.  Both are
+// for positive normal floats, 2^-126 <= x < 2^128: the exponent is rebiased
+// (1023 - 127 = 896) and the mantissa shifted by 29 bits, truncating x to 24
+// significant bits (a seed's argument) or extending f exactly.
+__device__ __forceinline__ float f32_from_pos(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
 }
 
-// Reciprocal and reciprocal cube root on the FP64 critical path.  A
-// dependent FP64 instruction costs one issue slot of its SM sub-partition
-// (64 cycles on GB300); the general-purpose division and rcbrt() take about
-// 6 and 18 of them.  Both here start from a hardware seed and take one
-// third-order Newton step (the truncated binomial series of (1 - e)^(-1/p)
-// for the seed's relative residual e), which cubes the seed's relative error:
+__device__ __forceinline__ double f64_from_pos(float f)
+{
+    const unsigned fb = __float_as_uint(f);
+    return __hiloint2double((int)((fb >> 3) + (896u << 20)), (int)(fb << 29));
+}
+
+// x^p (p = -1/3, -1/8) of a positive float from the special-function unit:
+// 2^(p log2 x), relative error about 2^-21 (a seed, never a result)
+__device__ __forceinline__ float f32_pow_seed(float x, float p)
+{
+    float l, y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(p * l));
+    return y;
+}
+#endif
+
+// Reciprocal, reciprocal square root, reciprocal cube root and the step
+// controller's x^(-1/8) on the FP64 critical path.  A dependent FP64
+// instruction costs one issue slot of its SM sub-partition (64 cycles on
+// GB300); the general-purpose division, rsqrt() and rcbrt() take about 6, 6
+// and 18 of them.  Each here starts from a seed and takes one third-order
+// Newton step (the truncated binomial series of (1 - e)^(-1/p) for the seed's
+// relative residual e), which cubes the seed's relative error:
 //
-//   1/x:       y0 = rcp.approx.ftz.f64(x) (rel. error < 2^-19),
-//              e = 1 - x y0,      y = y0 (1 + e + e^2)
-//   x^(-1/3):  y0 = x^(-1/3) in single precision (rel. error ~2^-22),
-//              e = 1 - x y0^3,    y = y0 (1 + e/3 + 2 e^2 / 9)
+//   1/x:        y0 = rcp.approx.ftz.f64(x)   (rel. error < 2^-19),
+//               e = 1 - x y0,      y = y0 (1 + e + e^2)
+//   1/sqrt(x):  y0 = rsqrt.approx.ftz.f64(x),
+//               e = 1 - x y0^2,    y = y0 (1 + e/2 + 3 e^2/8)
+//   x^(-1/3):   y0 = 2^(-log2(x)/3) in single precision,
+//               e = 1 - x y0^3,    y = y0 (1 + e/3 + 2 e^2/9)
+//   x^(-1/8):   y0 = 2^(-log2(x)/8) in single precision,
+//               e = 1 - x y0^8,    y = y0 (1 + e/8 + 9 e^2/128)
 //
-// Measured against the device's division and rcbrt() and extended-precision
-// references over 10^6 arguments in [1e-6, 1e6]: within 0.51 and 0.77 ulp.
-// Arguments are finite, nonzero and of normal range on the hot path (r >= 1,
-// D_c ~ 1, 1 - e^(-m x) in (0, 1), omega in (0, 1)); x = 0 or x = inf give
-// NaN, which the integrator's finiteness checks report, and the cube root's
-// single-precision seed needs |x| within the float range (1e-38 .. 3e38;
-// orbital frequencies are above 1e-6).  Host: 1/x and 1/cbrt(x).
+// The two FP64 seeds carry about 20 significant bits (their low words are
+// zero), so y0^2 is exact and e is formed with a single rounding.  Measured
+// against extended-precision references over 2.6e5 arguments in [1e-6, 1e6]
+// (tests/test_gpu_math.py): within one ulp each.  Arguments are positive and
+// of normal range on the hot path (r >= 1, D_c ~ 1, A W ~ 1, 1 - e^(-m x) in
+// (0, 1), omega in (0, 1)); x = 0 or x = inf give NaN or inf, which the
+// integrator's finiteness checks report, and the single-precision seeds need
+// 2^-126 <= x < 2^128 (orbital frequencies are above 1e-6).  Host: the
+// library's 1/x, 1/sqrt(x), 1/cbrt(x).
 EOB_HD double eob_rcp(double x)
 {
 #ifdef __CUDA_ARCH__
@@ -55,10 +82,22 @@ EOB_HD double eob_rcp(double x)
 #endif
 }
 
+EOB_HD double eob_rsqrt(double x)
+{
+#ifdef __CUDA_ARCH__
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, y * y, 1.0);
+    return fma(y * e, fma(e, 0.375, 0.5), y);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
 EOB_HD double eob_rcbrt(double x)
 {
 #ifdef __CUDA_ARCH__
-    const double y = (double)rcbrtf((float)x);
+    const double y = f64_from_pos(f32_pow_seed(f32_from_pos(x), -1.0f / 3.0f));
     const double e = fma(-x, y * y * y, 1.0);
     return fma(y * e, fma(e, 2.0 / 9.0, 1.0 / 3.0), y);
 #else
@@ -66,23 +105,77 @@ EOB_HD double eob_rcbrt(double x)
 #endif
 }
 
-// x^(-1/8) (the step-size controller's err^(-1/8)) without pow(): a
-// single-precision seed (FP32 pipe) refined by one third-order step for
-// y^-8 = x, e = 1 - x y^8, y <- y (1 + e/8 + 9 e^2/128): 7 FP64 instructions
-// instead of a reciprocal square root and two square roots (about 24).  x is
-// first clamped to [1e-30, 1e30] (NaN passes through): the controller clamps
-// the resulting scale to [1/3, 6], which every x outside that range reaches
-// anyway.  Host: 1/sqrt(sqrt(sqrt(x))) of the clamped x.
+// x^(-1/8) without pow(): 7 FP64 instructions instead of a reciprocal square
+// root and two square roots (about 24).  x is first clamped to [1e-30, 1e30]
+// (NaN passes through), by integer comparisons of its bits (a comparison of
+// doubles takes an FP64 issue slot): the controller clamps the resulting
+// scale to [1/3, 6], which every x outside that range reaches anyway.  Host:
+// 1/sqrt(sqrt(sqrt(x))) of the clamped x.
 EOB_HD double eob_inv_eighth_root(double x)
 {
-    x = (x < 1e-30) ? 1e-30 : ((x > 1e30) ? 1e30 : x);
 #ifdef __CUDA_ARCH__
-    const double y = (double)rsqrtf(sqrtf(sqrtf((float)x)));
+    const long long b = __double_as_longlong(x);
+    constexpr long long kLo = 0x39b4484bfeebc2a0LL;  // bits of 1e-30
+    constexpr long long kHi = 0x46293e5939a08ceaLL;  // bits of 1e30
+    constexpr long long kInf = 0x7ff0000000000000LL;
+    // b < kLo: below 1e-30 or negative (or a NaN with the sign bit set,
+    // which makes the scale finite; the caller ends the pass on err's NaN)
+    x = (b < kLo) ? 1e-30 : ((b > kHi && b <= kInf) ? 1e30 : x);
+    const double y = f64_from_pos(f32_pow_seed(f32_from_pos(x), -0.125f));
     const double y2 = y * y, y4 = y2 * y2;
     const double e = fma(-x, y4 * y4, 1.0);
     return fma(y * e, fma(e, 9.0 / 128.0, 0.125), y);
 #else
+    x = (x < 1e-30) ? 1e-30 : ((x > 1e30) ? 1e30 : x);
     return 1.0 / sqrt(sqrt(sqrt(x)));
+#endif
+}
+
+// e^(-y) - 1 for 0 <= y < 700 (the m factors' arguments 4 pi m H omega lie
+// in (0, 40)) by the table-driven method of P. T. P. Tang (ACM TOMS 15, 144
+// (1989)): -y = (32 n + j) ln2/32 + r with |r| <= ln2/64, so that
+// e^(-y) = 2^n 2^(j/32) e^r, e^r - 1 by its Taylor polynomial of degree 7
+// (truncation below 5e-17 relative), the 32 values 2^(j/32) from a table
+// (correctly rounded).  For n = j = 0 the polynomial is the result (S = 1
+// below), with no cancellation in e^(-y) - 1; otherwise the result is within
+// about 1.4e-16 in absolute terms (6e-15 relative to 1 - e^(-y) >= 0.0107:
+// the table entry's rounding, that of S - 1 and of the last fma).  12 FP64
+// instructions; exp() measures about 1150 cycles on GB300, 18 FP64 issue
+// slots.  Host: expm1(-y).
+#define EOB_EXP2_32_INIT                                                                                         \
+    {0x1.0000000000000p+0, 0x1.059b0d3158574p+0, 0x1.0b5586cf9890fp+0, 0x1.11301d0125b51p+0, 0x1.172b83c7d517bp+0, \
+     0x1.1d4873168b9aap+0, 0x1.2387a6e756238p+0, 0x1.29e9df51fdee1p+0, 0x1.306fe0a31b715p+0, 0x1.371a7373aa9cbp+0, \
+     0x1.3dea64c123422p+0, 0x1.44e086061892dp+0, 0x1.4bfdad5362a27p+0, 0x1.5342b569d4f82p+0, 0x1.5ab07dd485429p+0, \
+     0x1.6247eb03a5585p+0, 0x1.6a09e667f3bcdp+0, 0x1.71f75e8ec5f74p+0, 0x1.7a11473eb0187p+0, 0x1.82589994cce13p+0, \
+     0x1.8ace5422aa0dbp+0, 0x1.93737b0cdc5e5p+0, 0x1.9c49182a3f090p+0, 0x1.a5503b23e255dp+0, 0x1.ae89f995ad3adp+0, \
+     0x1.b7f76f2fb5e47p+0, 0x1.c199bdd85529cp+0, 0x1.cb720dcef9069p+0, 0x1.d5818dcfba487p+0, 0x1.dfc97337b9b5fp+0, \
+     0x1.ea4afa2a490dap+0, 0x1.f50765b6e4540p+0}
+#ifdef __CUDACC__
+__device__ const double kExp2_32[32] = EOB_EXP2_32_INIT;
+#endif
+
+EOB_HD double eob_expm1_neg(double y)
+{
+#ifdef __CUDA_ARCH__
+    constexpr double kShift = 6755399441055744.0;        // 1.5 2^52: round to integer in the low bits
+    constexpr double kInvL = 0x1.71547652b82fep+5;       // 32 / ln 2
+    constexpr double kLHi = 0x1.62e42fefa2000p-6;        // ln2/32, 40 significant bits
+    constexpr double kLLo = 0x1.9ef35793c7673p-46;       // ln2/32 - kLHi
+    const double t = fma(-y, kInvL, kShift);
+    const double nd = t - kShift;                        // N = round(-y 32 / ln 2)
+    const double r = fma(nd, -kLLo, fma(nd, -kLHi, -y));
+    const int N = (int)__double2loint(t);                // two's complement N in the low word
+    double q = fma(r, 1.0 / 5040.0, 1.0 / 720.0);
+    q = fma(q, r, 1.0 / 120.0);
+    q = fma(q, r, 1.0 / 24.0);
+    q = fma(q, r, 1.0 / 6.0);
+    q = fma(q, r, 0.5);
+    const double p = fma(r * r, q, r);                   // e^r - 1 to degree 7
+    // 2^n 2^(j/32) by adding n to the table entry's exponent field
+    const double S = __longlong_as_double(__double_as_longlong(kExp2_32[N & 31]) + ((long long)(N >> 5) << 52));
+    return fma(S, p, S - 1.0);                           // p itself when N = 0 (S = 1)
+#else
+    return expm1(-y);
 #endif
 }
 

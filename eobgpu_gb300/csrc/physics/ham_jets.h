@@ -43,6 +43,7 @@ enum JetId : int {
 struct HamJets {
     double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
     double n4, apsq, nu, M;
+    double inv8pinu;  // 1 / (8 pi nu): the flux's factor omega / (8 pi nu)
     // The log r and sqrt(u) polynomials have one or two adjacent terms per
     // jet: L = u^k (a + b u) with k = lk (3..5) and lc = {a, b, k a, (k+1) b};
     // S = s u^k with k = sk (2..6) and sc = {s, k s} (zero where a jet has no
@@ -122,6 +123,7 @@ EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
     J->apsq = h.apsq;
     J->nu = h.nu;
     J->M = h.M;
+    J->inv8pinu = 1.0 / (8.0 * kPi * h.nu);
 }
 
 // powers of u for the sparse log r and sqrt(u) polynomials
@@ -371,6 +373,23 @@ EOB_HD HamPart comb_final(const HamJets &J, double u, const HeffPart &ev, const 
     const double nu = J.nu, M = J.M;
     const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
     const double rs = eob_rsqrt(s2);
+    const double s = s2 * rs;
+    const double f = M * rs;
+    HamPart o;
+    o.H = M * s / nu;
+    o.Hreal = M * s;
+    o.dHdr = -(u * u) * f * (ev.du + od.du);
+    o.dHdpr = f * (ev.dp + od.dp);
+    o.dHdL = f * (ev.dL + od.dL);
+    return o;
+}
+
+// comb_final from s^2 = 1 + 2 nu (H_eff - 1) and 1/s computed elsewhere
+// (the four-warp group takes them from the warp that forms H_eff)
+EOB_HD HamPart comb_final_s(const HamJets &J, double u, const HeffPart &ev, const HeffPart &od, double s2,
+                            double rs)
+{
+    const double nu = J.nu, M = J.M;
     const double s = s2 * rs;
     const double f = M * rs;
     HamPart o;

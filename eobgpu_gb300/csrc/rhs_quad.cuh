@@ -5,17 +5,19 @@
 //
 //   stage           warp 0              warp 1              warp 2              warp 3
 //   jets            log r               polynomial parts    sqrt(u) polynomials log polynomials
-//                                                           and sqrt(u)
+//                                                                               and sqrt(u)
 //   combination a   1/Dc, A(u)          1/Dc, c(u),         B_np, q, W - L^2 c  N(u, p_r^2)
 //                                       q part of dW/dp_r
-//   combination b   even part sqrt(AW)  odd part            --                  y_2/y_3, 1/(8 pi nu)
-//   H, flux set-up  H and gradient,     m factors from      omega, v = omega    omega, log v,
-//                   v_phi^2             H_real omega = M^2 D r_omega^2, v^12, S_o H_real, S_even
+//   combination b   even part sqrt(AW)  odd part            H_eff's value,      y_2/y_3
+//                   and derivatives     and derivatives     s^2, 1/s
+//   H, flux set-up  H and gradient,     m x/(1-e^{-m x})    omega, v = omega    omega, log v,
+//                   v_phi^2, 4 k^2      from H_real omega   r_omega^2, v^12, S_o H_real, S_even
+//                                       = M^2 D
 //   multipoles      series part 0..15   m-factor and v_phi  series part 16..34  m-factor and v_phi
 //                   (two lanes each)    part 0..31                              part 32..34
-//   (then each multipole's two parts multiplied and summed)
+//   (then each multipole's two parts multiplied and summed by every warp)
 //
-// Values cross through shared memory at six barriers per right-hand side
+// Values cross through shared memory at five barriers per right-hand side
 // (an mbarrier of 128 arrivals with the pair's time limit).  As for the pair,
 // every value more than one warp uses afterwards is read by all of them from
 // shared memory, so the four warps' results and control decisions agree bit
@@ -34,23 +36,46 @@ struct QuadXchg {
     double pw[3][32];      // warp 2: W - L^2 c and its u-derivative, the B_np part of dW/dp_r
     double pwq[32];        // warp 1: the q part of dW/dp_r
     double pn[3][32];      // warp 3: N, dN/du, dN/dp_r^2
-    double ev[4][32];      // warp 0: even part of H_eff and its derivatives
-    double od[4][32];      // warp 1: odd part
+    double idc[32];        // warp 0: 1 / D_c
+    double hs[2][32];      // warp 2: s^2 = 1 + 2 nu (H_eff - 1) and 1/s
+    double ev[4][32];      // warp 0: derivatives of the even part of H_eff ([0] unused)
+    double od[4][32];      // warp 1: derivatives of the odd part ([0] unused)
     double ham[3];         // warp 0: dH/dr, dH/dp_r, dH/dL at the state
     double fl[16];         // v, log v, v^12, S_e^2, S_o^2, v_phi^2, v^5, v^2
     double T[8], k4[8];    // warp 1: m factors, m = 1..8
-    double b[40];          // m-factor parts of the multipoles (sorted positions)
-    double part[2];        // flux partial sums (warps 0 and 2)
-    double aux[2];         // warp 3: y_2 / y_3, 1 / (8 pi nu)
+    double b[64];          // warps 1, 3: m-factor parts of the multipoles (sorted positions 0..34)
+    double a[64];          // warps 0, 2: series parts (positions 0..34)
+    double aux[1];         // warp 3: y_2 / y_3
     unsigned long long slot;
 };
 
 constexpr int kQuadMax = 2;  // quads per block (256 threads)
 
+// Per-lane constants of a four-warp group, set once per launch: the
+// multipole whose series part (warps 0, 2) or m-factor part (warps 1, 3) the
+// lane evaluates, and m as a double for the m-factor lanes (lanes 0..7 give
+// m = 1..8).  Kept in registers: the lookups would otherwise be chained
+// global loads at the start of every multipole phase.
+struct QuadLane {
+    int i, lm;  // kFluxOrder at the lane's sorted position, lm_packed(i)
+    double md;  // (lane & 7) + 1
+};
+
+__device__ __forceinline__ QuadLane quad_lane(int q, int lane)
+{
+    int pos = (q == 0) ? (lane & 15) : (q == 2) ? 16 + lane : (q == 1) ? lane : 32 + lane;
+    pos = pos < kNumLM ? pos : kNumLM - 1;
+    QuadLane o;
+    o.i = kFluxOrder[pos];
+    o.lm = lm_packed(o.i);
+    o.md = (double)((lane & 7) + 1);
+    return o;
+}
+
 // k = f(y) for the binary of this quad; the four warps call it with the same y
 // and return the same k.  q: warp of the quad (0..3); lane: 0..31.
-__device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &t, const double y[4], double k[4],
-                                             int lane, int q, QuadXchg &x, PairSync &ps)
+__device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &t, const QuadLane &ql, const double y[4],
+                                             double k[4], int lane, int q, QuadXchg &x, PairSync &ps)
 {
     const double r = y[0], L = y[3];
     const int j = lane & 15;
@@ -65,19 +90,19 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         x.jet[1][0][lane] = p.v;
         x.jet[1][1][lane] = p.d;
     } else if (q == 2) {
-        // sqrt(u) = 1/sqrt(r), beside the division u = 1/r
-        const double su = eob_rsqrt(r);
         const Jet p = jet_poly_s(J, j, upow(u));
         x.jet[2][0][lane] = p.v;
         x.jet[2][1][lane] = p.d;
+    } else {
+        // sqrt(u) = 1/sqrt(r) beside the log polynomials
+        const double su = eob_rsqrt(r);
+        const Jet p = jet_poly_l(J, j, upow(u));
+        x.jet[0][0][lane] = p.v;
+        x.jet[0][1][lane] = p.d;
         if (lane == 0) {
             x.su[0] = su;
             x.su[1] = 0.5 * r * su;
         }
-    } else {
-        const Jet p = jet_poly_l(J, j, upow(u));
-        x.jet[0][0][lane] = p.v;
-        x.jet[0][1][lane] = p.d;
     }
     pair_sync(ps);  // 1: jets
     // poly + sqrt(u) poly + log r * log poly, the same expression on every
@@ -100,6 +125,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         jt[J_Q8].v = __shfl_sync(0xffffffffu, jv, J_Q8);
     } else if (q == 2) {
         gather(J_AK0); gather(J_DB); gather(J_G); gather(J_BX); gather(J_Q4); gather(J_Q6); gather(J_Q8);
+        jt[J_DC].v = __shfl_sync(0xffffffffu, jv, J_DC);
     } else {
         gather(J_N0); gather(J_N1); gather(J_N2); gather(J_N3);
     }
@@ -112,6 +138,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const PartA a = comb_A(jt, idc);
         x.pa[0][lane] = a.Av;
         x.pa[1][lane] = a.Ad;
+        x.idc[lane] = idc;
     } else if (q == 1) {
         idc = eob_rcp(jt[J_DC].v);
         const PartC c = comb_C(J, jt, u, idc);
@@ -134,40 +161,52 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const PartA a{x.pa[0][lane], x.pa[1][lane]};
         const PartC c{x.pc[0][lane], x.pc[1][lane]};
         const PartW w{x.pw[0][lane], x.pw[1][lane], x.pw[2][lane] + x.pwq[lane]};
-        const HeffPart e = comb_even_parts(a, c, w, L);
-        x.ev[0][lane] = e.v;
+        const HeffPart e = comb_even_parts(a, c, w, L);  // its value: warp 2
         x.ev[1][lane] = e.du;
         x.ev[2][lane] = e.dp;
         x.ev[3][lane] = e.dL;
     } else if (q == 1) {
         const PartN n{x.pn[0][lane], x.pn[1][lane], x.pn[2][lane]};
-        const HeffPart o = comb_odd_parts(jt, u, idc, n, pr, L);
-        x.od[0][lane] = o.v;
+        const HeffPart o = comb_odd_parts(jt, u, idc, n, pr, L);  // its value: warp 2
         x.od[1][lane] = o.du;
         x.od[2][lane] = o.dp;
         x.od[3][lane] = o.dL;
-    } else if (q == 3 && lane == 0) {
-        // written after barrier 1 of this right-hand side, so no warp still
-        // reads the previous values (they are read after barrier 6)
+    } else if (q == 2) {
+        // H_eff's value from the same pieces as warps 0 and 1 (even part
+        // sqrt(A W), odd part L u^3 N / D_c), then s^2 and 1/s, which the
+        // H and flux set-up of every warp needs after barrier 3
+        const double W = fma(L * L, x.pc[0][lane], x.pw[0][lane]);
+        const double AW = x.pa[0][lane] * W;
+        const double ev = AW * eob_rsqrt(AW);
+        const double u3i = (u * u * u) * x.idc[lane];
+        const double od = L * u3i * x.pn[0][lane];
+        const double s2 = fma(2.0 * J.nu, (ev + od) - 1.0, 1.0);
+        x.hs[0][lane] = s2;
+        x.hs[1][lane] = eob_rsqrt(s2);
+    } else if (lane == 0) {
+        // written after barrier 2 of this right-hand side, so no warp still
+        // reads the previous value (it is read between barriers 5 and 6)
         x.aux[0] = y[2] / y[3];
-        x.aux[1] = 1.0 / (8.0 * kPi * J.nu);
     }
-    pair_sync(ps);  // 3: even and odd parts
+    pair_sync(ps);  // 3: even and odd parts, s^2 and 1/s
 
     // ---- H and the flux set-up
     // lane 0's (state) parts: D = dH_eff/dL
     const double D = x.ev[3][0] + x.od[3][0];
     if (q == 0) {
         HeffPart ev, od;
-        ev.v = x.ev[0][lane];
+        ev.v = 0.0;  // H_eff's value enters through s^2 and 1/s
         ev.du = x.ev[1][lane];
         ev.dp = x.ev[2][lane];
         ev.dL = x.ev[3][lane];
-        od.v = x.od[0][lane];
+        od.v = 0.0;
         od.du = x.od[1][lane];
         od.dp = x.od[2][lane];
         od.dL = x.od[3][lane];
-        const HamPart hp = comb_final(J, u, ev, od);
+        const HamPart hp = comb_final_s(J, u, ev, od, x.hs[0][lane], x.hs[1][lane]);
+        // 4 k^2 = 4 (m H_real omega)^2 of the m factors, H_real omega = M^2 D
+        const double k4m = flux_m_factor_k4(ql.md, (J.M * J.M) * D);
+        if (lane < 8) x.k4[lane] = k4m;
         const double omega = __shfl_sync(0xffffffffu, hp.dHdL, 0);
         const double omega_c = __shfl_sync(0xffffffffu, hp.dHdL, 1);
         if (lane == 0) {
@@ -181,20 +220,14 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const double vphi = omega * (rc * rc);
         if (lane == 0) x.fl[5] = vphi * vphi;
     } else if (q == 1) {
-        // H_real omega = M^2 D (H_real = M s, omega = M D / s)
-        const double hw = (J.M * J.M) * D;
-        double Tm, k4m;
-        flux_m_factors((lane & 7) + 1, 4.0 * kPi * hw, hw, &Tm, &k4m);
-        if (lane < 8) {
-            x.T[lane] = Tm;
-            x.k4[lane] = k4m;
-        }
+        // m x / (1 - e^{-m x}), x = 4 pi H_real omega = 4 pi M^2 D
+        // (H_real = M s, omega = M D / s)
+        const double Tm = flux_m_factor_T(ql.md, 4.0 * kPi * ((J.M * J.M) * D));
+        if (lane < 8) x.T[lane] = Tm;
     } else {
-        // s = sqrt(s2) and omega = M D / s from the state's parts
-        const double heff = x.ev[0][0] + x.od[0][0];
-        const double s2 = fma(2.0 * J.nu, heff - 1.0, 1.0);
-        const double rs = eob_rsqrt(s2);
-        const double omega = (J.M * D) * rs;
+        // omega = M D / s at the state
+        const double s2 = x.hs[0][0];
+        const double omega = (J.M * D) * x.hs[1][0];
         if (q == 2) {
             // v = omega^(1/3) = omega r^2, v^12, S_odd = v p_phi
             const double ro = eob_rcbrt(omega);
@@ -235,38 +268,35 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     if (q == 0) {
         // positions 0..15 (degree 10 .. 4): lanes j and j + 16 take the two
         // halves of rho's series of position j
-        const int i = kFluxOrder[lane & 15];
-        const double hv = flux_rho_half(t, i, f, lane >> 4);
+        const double hv = flux_rho_half_m(t, ql.i, ql.lm & 15, f, lane >> 4);
         const double hi = __shfl_xor_sync(0xffffffffu, hv, 16);
         const double rho = fma(fma(x.fl[6], hi, hv), f.v, 1.0);
-        a_part = flux_mode_s_rho(t, i, f, rho);
+        const double a_part = flux_mode_s_rho_lm(t, ql.i, ql.lm, f, rho);
+        if (lane < 16) x.a[lane] = a_part;
     } else if (q == 2) {
         // positions 16..34 (degree 4 .. 2)
         const int pos = 16 + lane;
-        a_part = flux_mode_s<kFluxDegSorted[16]>(t, kFluxOrder[pos < kNumLM ? pos : kNumLM - 1], f);
+        const double a_part = flux_mode_s_lm<kFluxDegSorted[16]>(t, ql.i, ql.lm, f);
+        if (pos < kNumLM) x.a[pos] = a_part;
     } else {
         const int pos = (q == 1) ? lane : 32 + lane;
         if (pos < kNumLM) {
-            const int i = kFluxOrder[pos];
-            const int m = lm_packed(i) & 15;
-            x.b[pos] = flux_mode_b(t, i, x.T[m - 1], x.k4[m - 1]) * flux_mode_vp_sq(i, x.fl[5]);
+            const int m = ql.lm & 15;
+            x.b[pos] = flux_mode_b_l(t, ql.i, ql.lm >> 4, x.T[m - 1], x.k4[m - 1]) * flux_mode_vp_sq_lm(ql.lm, x.fl[5]);
         }
     }
-    pair_sync(ps);  // 5: m-factor parts
+    pair_sync(ps);  // 5: series and m-factor parts
     // F / omega = total c1 with F = total omega^2 / (8 pi) / nu, and
-    // (y_2 / y_3) F / omega = total c2: the factors are taken here, beside
-    // the reduction below, so that only two products follow the last barrier
+    // (y_2 / y_3) F / omega = total c2
     const double omega = x.ham[2];
-    const double c1 = omega * x.aux[1], c2 = x.aux[0] * c1;
-    if (q == 0 || q == 2) {
-        const int pos = (q == 0) ? lane : 16 + lane;
-        double part = (q == 0 ? lane < 16 : pos < kNumLM) ? x.b[pos] * a_part : 0.0;
+    const double c1 = omega * J.inv8pinu, c2 = x.aux[0] * c1;
+    // every warp forms the total itself -- the same products and butterfly
+    // on the same shared values, so the same bits on every warp -- and no
+    // barrier follows: lane l takes positions l and (l < 3) 32 + l
+    const bool hi3 = lane < kNumLM - 32;
+    double total = fma(hi3 ? x.b[32 + lane] : 0.0, hi3 ? x.a[32 + lane] : 0.0, x.b[lane] * x.a[lane]);
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-        if (lane == 0) x.part[q >> 1] = part;
-    }
-    pair_sync(ps);  // 6: flux partial sums
-    const double total = x.part[0] + x.part[1];
+    for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(0xffffffffu, total, off);
     k[0] = x.ham[1];
     k[1] = omega;
     k[2] = -fma(c2, total, x.ham[0]);

@@ -300,9 +300,10 @@ int eob_fd_lnl_from_fft(const double *H, int N, int start_ind, const double *dat
  * the device's FP64 peak used as the integrator's roofline. */
 int eob_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream);
 /* Accuracy probe of the hot path's math: for each of the n device doubles x,
- * out[8 i + 0..7] = the hot path's reciprocal, the device division 1/x, the
+ * out[10 i + 0..9] = the hot path's reciprocal, the device division 1/x, the
  * hot path's x^(-1/3), the device rcbrt, the hot path's log, the device log,
- * the hot path's 1/sqrt(x), the step controller's x^(-1/8); out: device, 8 n
+ * the hot path's 1/sqrt(x), the step controller's x^(-1/8), the m factors'
+ * e^(-y) - 1 and the device expm1(-y) at y = min(x, 600); out: device, 10 n
  * doubles. */
 int eob_math_probe(const double *x, int n, double *out, cudaStream_t stream);
 /* The integrator's multi-warp group barrier with its wait limited to limit_ns

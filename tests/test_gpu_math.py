@@ -35,11 +35,11 @@ def test_hot_path_math_accuracy(torch_cuda):
                         rng.uniform(0.5, 2.0, n // 4),                           # one binade and its neighbours
                         rng.uniform(1.0, 40.0, n // 4)])                         # radii of the trajectories
     xd = torch.tensor(x, device="cuda")
-    out = torch.empty(8 * n, dtype=torch.float64, device="cuda")
+    out = torch.empty(10 * n, dtype=torch.float64, device="cuda")
     rc = lib.eob_math_probe(ctypes.c_void_p(xd.data_ptr()), n, ctypes.c_void_p(out.data_ptr()), None)
     assert rc == 0
     torch.cuda.synchronize()
-    o = out.cpu().numpy().reshape(n, 8)
+    o = out.cpu().numpy().reshape(n, 10)
     xl = x.astype(np.longdouble)
     # reciprocal: faithful (within one ulp), and equal to the division in almost every case
     np.testing.assert_array_equal(o[:, 1], 1.0 / x)
@@ -61,3 +61,17 @@ def test_hot_path_math_accuracy(torch_cuda):
     # the step controller's x^(-1/8) (arguments inside its clamp [1e-30, 1e30])
     u = _ulps(o[:, 7], 1 / np.sqrt(np.sqrt(np.sqrt(xl))))
     assert u.max() < 1.0, u.max()
+    # the m factors' e^(-y) - 1 (y = min(x, 600)): within 1.5e-16 absolute
+    # of the extended-precision value (the table entry's rounding, the
+    # rounding of S - 1 and of the last fma; at most 6e-15 relative to
+    # 1 - e^(-y) >= 0.0107), and within 2 ulp where y < ln2/64 (no
+    # cancellation there)
+    y = np.minimum(xl, 600)
+    ref = np.expm1(-y)
+    err = np.abs(o[:, 8].astype(np.longdouble) - ref)
+    assert err.max() < 1.5e-16, float(err.max())
+    assert np.max(err / np.abs(ref)) < 6e-15, float(np.max(err / np.abs(ref)))
+    small = np.asarray(y < np.log(2) / 64)
+    assert small.sum() > 1000
+    assert _ulps(o[small, 8], ref[small]).max() <= 2.0
+    np.testing.assert_allclose(o[:, 8], o[:, 9], rtol=6e-15, atol=1.5e-16)
