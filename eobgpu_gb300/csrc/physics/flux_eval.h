@@ -536,11 +536,10 @@ EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, doub
     return flux_mode_s_rho_lm(t, i, lm_packed(i), f, rho);
 }
 
+// elm = eulerlog_m(v) = elog[m] + log v, passed by callers that form it once per m
 template <int KMAX>
-EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &f)
+EOB_HD double flux_mode_s_e(const FluxTable &t, int i, int lm, double elm, const FluxLane &f)
 {
-    const int m = lm & 15;
-    const double elm = t.elog[m] + f.lv;
     // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
     double acc = t.rho[i][KMAX];
     if (KMAX == 6 || KMAX == 7 || KMAX == 8 || KMAX == 10) acc = fma(t.rhol[i][KMAX], elm, acc);
@@ -554,6 +553,12 @@ EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &
 }
 
 template <int KMAX>
+EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &f)
+{
+    return flux_mode_s_e<KMAX>(t, i, lm, t.elog[lm & 15] + f.lv, f);
+}
+
+template <int KMAX>
 EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
 {
     return flux_mode_s_lm<KMAX>(t, i, lm_packed(i), f);
@@ -563,9 +568,8 @@ EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
 // c_1 + c_2 v + ... + c_5 v^4 and half 1 gives c_6 + c_7 v + ... + c_10 v^4,
 // c_k = rho_k + rhol_k eulerlog_m (rhol_k is zero where the series has no
 // log term); then rho = 1 + v (half 0 + v^5 half 1)
-EOB_HD double flux_rho_half_m(const FluxTable &t, int i, int m, const FluxLane &f, int half)
+EOB_HD double flux_rho_half_e(const FluxTable &t, int i, double elm, const FluxLane &f, int half)
 {
-    const double elm = t.elog[m] + f.lv;
     const double *rh = t.rho[i] + (half ? 6 : 1), *rl = t.rhol[i] + (half ? 6 : 1);
     double acc = fma(rl[4], elm, rh[4]);
 #pragma unroll
@@ -575,7 +579,7 @@ EOB_HD double flux_rho_half_m(const FluxTable &t, int i, int m, const FluxLane &
 
 EOB_HD double flux_rho_half(const FluxTable &t, int i, const FluxLane &f, int half)
 {
-    return flux_rho_half_m(t, i, lm_packed(i) & 15, f, half);
+    return flux_rho_half_e(t, i, t.elog[lm_packed(i) & 15] + f.lv, f, half);
 }
 
 // vphi^(2 (l + eps)) of multipole i selected from the precomputed powers

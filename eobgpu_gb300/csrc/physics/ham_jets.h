@@ -153,7 +153,8 @@ EOB_HD double upow_sel(const UPow &p, int k)
 EOB_HD Jet jet_poly_l(const HamJets &J, int j, const UPow &p)
 {
     const double *c = J.lc[j];
-    const double pk = upow_sel(p, J.lk[j] - 1);  // u^(k-1)
+    const int k1 = J.lk[j] - 1;  // 2..4 (ham_jets_build keeps lk in 3..5)
+    const double pk = (k1 == 2) ? p.u2 : ((k1 == 3) ? p.u3 : p.u4);  // u^(k-1)
     return {(pk * p.u) * fma(c[1], p.u, c[0]), pk * fma(c[3], p.u, c[2])};
 }
 
@@ -162,6 +163,15 @@ EOB_HD Jet jet_poly_s(const HamJets &J, int j, const UPow &p)
 {
     const double pk = upow_sel(p, J.sk[j] - 1);  // u^(k-1)
     return {(pk * p.u) * J.sc[j][0], pk * J.sc[j][1]};
+}
+
+// the sqrt(u) polynomial with d/du (sqrt(u) S) / sqrt(u) = S' + r S / 2 in
+// place of S', so that the join needs sqrt(u) alone (d sqrt(u)/du =
+// sqrt(u) r / 2)
+EOB_HD Jet jet_poly_s_t(const HamJets &J, int j, const UPow &p, double r)
+{
+    const Jet s = jet_poly_s(J, j, p);
+    return {s.v, fma(0.5 * r, s.v, s.d)};
 }
 
 // value and d/du of jet j at u (r = 1/u, lr = log r, su = sqrt(u)): the
@@ -286,9 +296,8 @@ EOB_HD PartW comb_W(const Jet *jt, const CombB &b, double pr)
 // comb_W with dW/dp_r cut in two, for four warps: comb_W_b keeps its B_np
 // part 2 p_r (1 + B_np) and comb_Wp_q gives the rest,
 // 2 p_r p_r^2 (2 q_4 + 3 p_r^2 q_6 + 4 p_r^4 q_8), from the jets alone
-EOB_HD PartW comb_W_b(const CombB &b, double pr)
+EOB_HD PartW comb_W_b_p2(const CombB &b, double pr, double p2)
 {
-    const double p2 = pr * pr;
     PartW o;
     o.W = fma(p2 * p2, b.qa, fma(p2, 1.0 + b.bnpv, 1.0));
     o.Wu = fma(p2 * p2, b.qad, p2 * b.bnpd);
@@ -296,11 +305,14 @@ EOB_HD PartW comb_W_b(const CombB &b, double pr)
     return o;
 }
 
-EOB_HD double comb_Wp_q(const Jet *jt, double pr)
+EOB_HD PartW comb_W_b(const CombB &b, double pr) { return comb_W_b_p2(b, pr, pr * pr); }
+
+EOB_HD double comb_Wp_q_p2(const Jet *jt, double pr, double p2)
 {
-    const double p2 = pr * pr;
     return 2.0 * pr * (p2 * fma(p2, fma(4.0 * p2, jt[J_Q8].v, 3.0 * jt[J_Q6].v), 2.0 * jt[J_Q4].v));
 }
+
+EOB_HD double comb_Wp_q(const Jet *jt, double pr) { return comb_Wp_q_p2(jt, pr, pr * pr); }
 
 // a piece of H_eff with its derivatives in u, p_r and L
 struct HeffPart {
@@ -313,7 +325,6 @@ EOB_HD HeffPart comb_even_parts(const PartA &a, const PartC &c, const PartW &w, 
     const double L2 = L * L;
     const double W = fma(L2, c.cuv, w.W);
     const double Wu = fma(L2, c.cud, w.Wu);
-    const double WL = 2.0 * L * c.cuv;
     // sqrt and the reciprocal from one reciprocal square root
     const double AW = a.Av * W;
     const double rAW = eob_rsqrt(AW);
@@ -322,7 +333,7 @@ EOB_HD HeffPart comb_even_parts(const PartA &a, const PartC &c, const PartW &w, 
     o.v = AW * rAW;
     o.du = fma(a.Ad, W, a.Av * Wu) * ih2;
     o.dp = a.Av * w.Wp * ih2;
-    o.dL = a.Av * WL * ih2;
+    o.dL = (a.Av * L) * (c.cuv * rAW);  // A W_L / (2 sqrt(A W)), W_L = 2 L c
     return o;
 }
 
@@ -441,6 +452,15 @@ EOB_HD Jet jet_part_l(const HamJets &J, int j, double u, double r, double lr)
 // a jet from its polynomial part p, the sqrt(u) and log polynomials s and l,
 // su = sqrt(u), hs = r su / 2 = d sqrt(u) / du and lr = log r:
 // value P + su S + lr L, d/du = P' + su S' + hs S - r L + lr L'
+// the same from jet_poly_s_t's sqrt part (st.d = S' + r S / 2): one fma less
+EOB_HD Jet jet_join_t(const Jet &p, const Jet &st, const Jet &l, double su, double lr, double r)
+{
+    Jet out;
+    out.v = fma(lr, l.v, fma(su, st.v, p.v));
+    out.d = fma(lr, l.d, fma(-r, l.v, fma(su, st.d, p.d)));
+    return out;
+}
+
 EOB_HD Jet jet_join_s(const Jet &p, const Jet &s, const Jet &l, double su, double hs, double lr, double r)
 {
     Jet out;

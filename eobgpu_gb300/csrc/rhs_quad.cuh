@@ -30,7 +30,7 @@ namespace eob {
 struct QuadXchg {
     double jet[3][2][32];  // jets: [log polynomial, polynomial, sqrt part][v, d][lane]
     double lr;             // warp 0: log r
-    double su[2];          // warp 2: sqrt(u) = 1/sqrt(r), r sqrt(u) / 2
+    double su;             // warp 3: sqrt(u) = 1/sqrt(r)
     double pa[2][32];      // warp 0: A, dA/du
     double pc[2][32];      // warp 1: c, dc/du
     double pw[3][32];      // warp 2: W - L^2 c and its u-derivative, the B_np part of dW/dp_r
@@ -42,7 +42,8 @@ struct QuadXchg {
     double od[4][32];      // warp 1: derivatives of the odd part ([0] unused)
     double ham[3];         // warp 0: dH/dr, dH/dp_r, dH/dL at the state
     double fl[16];         // v, log v, v^12, S_e^2, S_o^2, v_phi^2, v^5, v^2
-    double T[8], k4[8];    // warp 1: m factors, m = 1..8
+    double T[8], k4[8];    // warps 1, 0: m factors, m = 1..8
+    double elm[8];         // warp 3: eulerlog_m(v) = elog[m] + log v, m = 1..8
     double b[64];          // warps 1, 3: m-factor parts of the multipoles (sorted positions 0..34)
     double a[64];          // warps 0, 2: series parts (positions 0..34)
     double aux[1];         // warp 3: y_2 / y_3
@@ -80,6 +81,10 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     const double r = y[0], L = y[3];
     const int j = lane & 15;
     const double u = eob_rcp(r);
+    double u3 = 0.0;  // warp 2: u^3 from the jets' powers, for its H_eff value
+    // p_r and p_r^2 of the combination (odd lanes: p_r = 0, the circular frequency)
+    const double pr = (lane & 1) ? 0.0 : y[2];
+    const double p2 = pr * pr;
 
     // ---- jets (lanes 16..31 repeat lanes 0..15)
     if (q == 0) {
@@ -90,25 +95,24 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         x.jet[1][0][lane] = p.v;
         x.jet[1][1][lane] = p.d;
     } else if (q == 2) {
-        const Jet p = jet_poly_s(J, j, upow(u));
+        const UPow up = upow(u);
+        const Jet p = jet_poly_s_t(J, j, up, r);
         x.jet[2][0][lane] = p.v;
         x.jet[2][1][lane] = p.d;
+        u3 = up.u3;
     } else {
         // sqrt(u) = 1/sqrt(r) beside the log polynomials
         const double su = eob_rsqrt(r);
         const Jet p = jet_poly_l(J, j, upow(u));
         x.jet[0][0][lane] = p.v;
         x.jet[0][1][lane] = p.d;
-        if (lane == 0) {
-            x.su[0] = su;
-            x.su[1] = 0.5 * r * su;
-        }
+        if (lane == 0) x.su = su;
     }
     pair_sync(ps);  // 1: jets
     // poly + sqrt(u) poly + log r * log poly, the same expression on every
     // warp; each warp gathers only the jets its pieces read
-    const Jet jn = jet_join_s({x.jet[1][0][lane], x.jet[1][1][lane]}, {x.jet[2][0][lane], x.jet[2][1][lane]},
-                              {x.jet[0][0][lane], x.jet[0][1][lane]}, x.su[0], x.su[1], x.lr, r);
+    const Jet jn = jet_join_t({x.jet[1][0][lane], x.jet[1][1][lane]}, {x.jet[2][0][lane], x.jet[2][1][lane]},
+                              {x.jet[0][0][lane], x.jet[0][1][lane]}, x.su, x.lr, r);
     const double jv = jn.v, jd = jn.d;
     Jet jt[kNumJets];
     auto gather = [&](int s) {
@@ -131,7 +135,6 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     }
 
     // ---- combination (odd lanes at p_r = 0: the circular frequency)
-    const double pr = (lane & 1) ? 0.0 : y[2];
     double idc = 0.0;
     if (q == 0) {
         idc = eob_rcp(jt[J_DC].v);
@@ -144,14 +147,14 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const PartC c = comb_C(J, jt, u, idc);
         x.pc[0][lane] = c.cuv;
         x.pc[1][lane] = c.cud;
-        x.pwq[lane] = comb_Wp_q(jt, pr);
+        x.pwq[lane] = comb_Wp_q_p2(jt, pr, p2);
     } else if (q == 2) {
-        const PartW w = comb_W_b(comb_b(jt, pr * pr), pr);
+        const PartW w = comb_W_b_p2(comb_b(jt, p2), pr, p2);
         x.pw[0][lane] = w.W;
         x.pw[1][lane] = w.Wu;
         x.pw[2][lane] = w.Wp;
     } else {
-        const PartN n = comb_N(J, jt, pr * pr);
+        const PartN n = comb_N(J, jt, p2);
         x.pn[0][lane] = n.Nv;
         x.pn[1][lane] = n.Nu;
         x.pn[2][lane] = n.Np;
@@ -177,10 +180,9 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         // H and flux set-up of every warp needs after barrier 3
         const double W = fma(L * L, x.pc[0][lane], x.pw[0][lane]);
         const double AW = x.pa[0][lane] * W;
-        const double ev = AW * eob_rsqrt(AW);
-        const double u3i = (u * u * u) * x.idc[lane];
+        const double u3i = u3 * x.idc[lane];
         const double od = L * u3i * x.pn[0][lane];
-        const double s2 = fma(2.0 * J.nu, (ev + od) - 1.0, 1.0);
+        const double s2 = fma(2.0 * J.nu, fma(AW, eob_rsqrt(AW), od) - 1.0, 1.0);
         x.hs[0][lane] = s2;
         x.hs[1][lane] = eob_rsqrt(s2);
     } else if (lane == 0) {
@@ -246,6 +248,8 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
             // (no square root on that branch)
             const double Se = fma(fma(J.M * J.M, s2, -1.0), t.inv2eta, 1.0);
             const double lv = eob_log(omega) * (1.0 / 3.0);
+            const double elm = t.elog[(lane & 7) + 1] + lv;
+            if (lane < 8) x.elm[lane] = elm;
             if (lane == 0) {
                 x.fl[1] = lv;
                 x.fl[3] = Se * Se;
@@ -268,7 +272,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     if (q == 0) {
         // positions 0..15 (degree 10 .. 4): lanes j and j + 16 take the two
         // halves of rho's series of position j
-        const double hv = flux_rho_half_m(t, ql.i, ql.lm & 15, f, lane >> 4);
+        const double hv = flux_rho_half_e(t, ql.i, x.elm[(ql.lm & 15) - 1], f, lane >> 4);
         const double hi = __shfl_xor_sync(0xffffffffu, hv, 16);
         const double rho = fma(fma(x.fl[6], hi, hv), f.v, 1.0);
         const double a_part = flux_mode_s_rho_lm(t, ql.i, ql.lm, f, rho);
@@ -276,21 +280,20 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     } else if (q == 2) {
         // positions 16..34 (degree 4 .. 2)
         const int pos = 16 + lane;
-        const double a_part = flux_mode_s_lm<kFluxDegSorted[16]>(t, ql.i, ql.lm, f);
+        const double a_part = flux_mode_s_e<kFluxDegSorted[16]>(t, ql.i, ql.lm, x.elm[(ql.lm & 15) - 1], f);
         if (pos < kNumLM) x.a[pos] = a_part;
     } else {
         const int pos = (q == 1) ? lane : 32 + lane;
         if (pos < kNumLM) {
+            // times F / (omega total) = omega / (8 pi nu): the sum below is F / omega
             const int m = ql.lm & 15;
-            x.b[pos] = flux_mode_b_l(t, ql.i, ql.lm >> 4, x.T[m - 1], x.k4[m - 1]) * flux_mode_vp_sq_lm(ql.lm, x.fl[5]);
+            const double c1 = x.ham[2] * J.inv8pinu;
+            x.b[pos] = (flux_mode_b_l(t, ql.i, ql.lm >> 4, x.T[m - 1], x.k4[m - 1]) * flux_mode_vp_sq_lm(ql.lm, x.fl[5])) * c1;
         }
     }
     pair_sync(ps);  // 5: series and m-factor parts
-    // F / omega = total c1 with F = total omega^2 / (8 pi) / nu, and
-    // (y_2 / y_3) F / omega = total c2
-    const double omega = x.ham[2];
-    const double c1 = omega * J.inv8pinu, c2 = x.aux[0] * c1;
-    // every warp forms the total itself -- the same products and butterfly
+    // F / omega (the m-factor parts carry omega / (8 pi nu)); every warp
+    // forms it itself -- the same products and butterfly
     // on the same shared values, so the same bits on every warp -- and no
     // barrier follows: lane l takes positions l and (l < 3) 32 + l
     const bool hi3 = lane < kNumLM - 32;
@@ -298,9 +301,9 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(0xffffffffu, total, off);
     k[0] = x.ham[1];
-    k[1] = omega;
-    k[2] = -fma(c2, total, x.ham[0]);
-    k[3] = -(total * c1);
+    k[1] = x.ham[2];
+    k[2] = -fma(x.aux[0], total, x.ham[0]);  // (y_2 / y_3) F / omega
+    k[3] = -total;
 }
 
 }  // namespace eob
