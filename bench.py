@@ -543,6 +543,27 @@ def run_op(args, local):
         flops = _op_flops("FLOP_PER_OUTPUT_TDINTERP2_K5" if K == 5 else "FLOP_PER_OUTPUT_TDINTERP2_K1")
         work = f"{B} binaries x {N} samples, {K} mode(s): write 16 B, read index 4 B and time 8 B per sample, " \
                f"spline tables once; {flops} FP64 FLOP per sample (census)"
+    elif args.op == "fd_split":
+        # the fused frequency-domain likelihood of BBHWaveformTD.get_ll: one
+        # complex FFT per binary of N = 2^17 samples (h~_+ and h~_x recovered
+        # from it), three detectors, N/2 + 1 bins
+        from eobgpu_gb300 import fd as fdmod
+        nch, N = 3, 131072
+        Nf = N // 2 + 1
+        H = torch.randn((B, N), dtype=torch.complex128, generator=g).to(device)
+        data = torch.randn((nch, Nf), dtype=torch.complex128, generator=g).to(device)
+        psd = (torch.rand((nch, Nf), dtype=torch.float64, generator=g) + 0.5).to(device)
+        Fp, Fx = [torch.rand(nch * B, dtype=torch.float64, generator=g).to(device) for _ in range(2)]
+        tau = (0.02 * torch.rand(nch * B, dtype=torch.float64, generator=g) - 0.01).to(device)
+        scratch = torch.empty(int(fdmod._lib.load().eob_fd_lnl_scratch_bytes(B, N)), dtype=torch.uint8, device=device)
+
+        def once():
+            fdmod.fd_lnl_from_fft(H, data, psd, Fp, Fx, tau, 1.0 / 64.0, 0, scratch)
+        units = B * Nf * nch
+        byts = B * N * 16 + nch * Nf * 24 + B * 8
+        flops = _op_flops("FLOP_PER_OUTPUT_FD_SPLIT")
+        work = f"{B} binaries x {Nf} bins x {nch} detectors: the complex FFT (16 B per sample) read once, " \
+               f"data and 1/PSD per detector; {flops} FP64 FLOP per (binary, bin, detector) (census)"
     else:
         nch, N = 3, 65537
         hp = torch.randn(B * N, dtype=torch.complex128, generator=g).to(device)
@@ -753,8 +774,8 @@ def main():
                     help="longest binaries on four warps each beside groups of 8..64 lanes (-1: the library's choice)")
     ap.add_argument("--block", type=int, default=0, help="integrator threads per block (0: default)")
     ap.add_argument("--grid", type=int, default=0, help="integrator blocks (0: one wave of resident blocks)")
-    ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl"],
-                    help="time one reference-shaped kernel alone (mode synthesis TD2, or FD likelihood partials)")
+    ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl", "fd_split"],
+                    help="time one kernel alone: mode synthesis TD2, FD likelihood partials, or the fused split-FFT FD likelihood")
     ap.add_argument("--census", action="store_true",
                     help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
     args = ap.parse_args()

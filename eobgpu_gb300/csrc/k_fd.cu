@@ -12,14 +12,17 @@
 // on the fly -- the bins f < N/2 + 1 read H(f) from the lower half and
 // H(N - f) from the mirrored block of the upper half, so every element of H
 // is read once and h~_+, h~_x are never written -- then projects onto every
-// detector and accumulates the residual.  A second kernel sums each binary's
-// block partials in a fixed order (deterministic, no atomics).
+// detector and accumulates the residual.  The PSD enters as its reciprocal,
+// formed once per call (a division costs about six FP64 issue slots on GB300,
+// a product one).  A last kernel sums each binary's block partials in a fixed
+// order (deterministic, no atomics).
 #include "eob_device.cuh"
 
 namespace {
 
-constexpr int kFdBins = 1024;     // frequency bins per block (the reference's 1024-bin partials)
 constexpr int kFdThreads = 256;
+constexpr int kFdPerThread = 16;                      // bins per thread, kFdThreads apart
+constexpr int kFdBins = kFdThreads * kFdPerThread;    // frequency bins per block
 constexpr int kFdMaxChannels = 8;
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr double kSpeedOfLight = 299792458.0;  // m/s
@@ -86,41 +89,52 @@ __global__ void k_detector_response(const double *ra, const double *dec, const d
     }
 }
 
+// 1 / S_n for every (detector, bin)
+__global__ void k_fd_inv_psd(const double *psd, long long n, double *ipsd)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        ipsd[i] = 1.0 / psd[i];
+}
+
 // One block of kFdBins bins (f = df i, i < Nf = N / 2 + 1) of one binary:
-// sum over detectors of |d - (F+ h~_+ + Fx h~_x) e^{-2 pi i f tau}|^2 / S_n,
-// h~ zero below start_ind.  partial[blockIdx.x * B + b].
+// sum over the NCH detectors of |d - (F+ h~_+ + Fx h~_x) e^{-2 pi i f tau}|^2
+// / S_n, h~ zero below start_ind.  partial[blockIdx.x * B + b].  Each thread
+// takes kFdPerThread bins kFdThreads apart; the delay phase comes from one
+// sincos at its first bin and one for the step, then rotations (a sincos
+// costs tens of FP64 instructions).  NCH is a template argument so that the
+// per-detector values stay in registers.
+template <int NCH>
 __global__ void __launch_bounds__(kFdThreads) k_fd_split_lnl(const double2 *H, int N, int start_ind,
-                                                             const double2 *data, const double *psd,
+                                                             const double2 *data, const double *ipsd,
                                                              const double *Fplus, const double *Fcross,
-                                                             const double *tshift, double df, int B, int nch,
-                                                             double *partial)
+                                                             const double *tshift, double df, int B, double *partial)
 {
     __shared__ double warp_sum[kFdThreads / 32];
     const int Nf = N / 2 + 1;
     for (int b = blockIdx.y; b < B; b += gridDim.y) {
         const double2 *Hb = H + (size_t)b * N;
-        double fp[kFdMaxChannels], fx[kFdMaxChannels], s[kFdMaxChannels], co[kFdMaxChannels], sd[kFdMaxChannels],
-            cd[kFdMaxChannels];
+        double fp[NCH], fx[NCH], s[NCH], co[NCH], sd[NCH], cd[NCH];
         const int i0 = blockIdx.x * kFdBins + threadIdx.x;
-        for (int c = 0; c < nch; ++c) {
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
             fp[c] = Fplus[(size_t)c * B + b];
             fx[c] = Fcross[(size_t)c * B + b];
             const double tau = tshift[(size_t)c * B + b];
-            // e^{-2 pi i f tau} at the thread's first bin, then rotations by the
-            // step between its bins (kFdThreads apart)
             sincos(kTwoPi * (df * i0) * tau, &s[c], &co[c]);
             sincos(kTwoPi * (df * kFdThreads) * tau, &sd[c], &cd[c]);
         }
         double acc = 0.0;
-#pragma unroll
-        for (int q = 0; q < kFdBins / kFdThreads; ++q) {
+#pragma unroll 4
+        for (int q = 0; q < kFdPerThread; ++q) {
             const int i = i0 + q * kFdThreads;
-            if (q > 0)
-                for (int c = 0; c < nch; ++c) {
-                    const double cn = co[c] * cd[c] - s[c] * sd[c];
+            if (q > 0) {
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) {
+                    const double cn = fma(co[c], cd[c], -s[c] * sd[c]);
                     s[c] = fma(s[c], cd[c], co[c] * sd[c]);
                     co[c] = cn;
                 }
+            }
             if (i < Nf) {
                 double pr = 0.0, pi = 0.0, xr = 0.0, xi = 0.0;
                 if (i >= start_ind) {
@@ -132,12 +146,13 @@ __global__ void __launch_bounds__(kFdThreads) k_fd_split_lnl(const double2 *H, i
                     xr = 0.5 * (a.y + z.y);
                     xi = -0.5 * (a.x - z.x);
                 }
-                for (int c = 0; c < nch; ++c) {
-                    const double gr = fp[c] * pr + fx[c] * xr, gi = fp[c] * pi + fx[c] * xi;
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) {
+                    const double gr = fma(fp[c], pr, fx[c] * xr), gi = fma(fp[c], pi, fx[c] * xi);
                     const double2 d = data[(size_t)c * Nf + i];
-                    const double rr = d.x - (gr * co[c] + gi * s[c]);
-                    const double ri = d.y - (gi * co[c] - gr * s[c]);
-                    acc += (rr * rr + ri * ri) / psd[(size_t)c * Nf + i];
+                    const double rr = d.x - fma(gr, co[c], gi * s[c]);
+                    const double ri = d.y - fma(gi, co[c], -gr * s[c]);
+                    acc = fma(fma(rr, rr, ri * ri), ipsd[(size_t)c * Nf + i], acc);
                 }
             }
         }
@@ -187,11 +202,14 @@ int eob_detector_response(const double *ra, const double *dec, const double *psi
     return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 
+// block partials of every binary, then 1 / S_n for up to kFdMaxChannels
+// detectors (256-byte aligned)
 size_t eob_fd_lnl_scratch_bytes(int B, int N)
 {
     if (B < 1 || N < 2) return 0;
     const long long nblk = ((long long)(N / 2 + 1) + kFdBins - 1) / kFdBins;
-    return (size_t)(nblk * B) * sizeof(double);
+    const size_t part = ((size_t)(nblk * B) * sizeof(double) + 255) & ~(size_t)255;
+    return part + (size_t)kFdMaxChannels * (size_t)(N / 2 + 1) * sizeof(double);
 }
 
 int eob_fd_lnl_from_fft(const double *H, int N, int start_ind, const double *data, const double *psd,
@@ -203,9 +221,23 @@ int eob_fd_lnl_from_fft(const double *H, int N, int start_ind, const double *dat
     if (scratch_bytes < eob_fd_lnl_scratch_bytes(B, N)) return EOB_E_ARG;
     const int nblk = (N / 2 + 1 + kFdBins - 1) / kFdBins;
     double *partial = (double *)scratch;
+    const size_t part = ((size_t)nblk * (size_t)B * sizeof(double) + 255) & ~(size_t)255;
+    double *ipsd = (double *)((char *)scratch + part);
+    const long long npsd = (long long)nch * (N / 2 + 1);
+    k_fd_inv_psd<<<blocks_for(npsd, 256), 256, 0, stream>>>(psd, npsd, ipsd);
+    if (cudaGetLastError() != cudaSuccess) return EOB_E_CUDA;
     dim3 grid(nblk, B < 65535 ? B : 65535);
-    k_fd_split_lnl<<<grid, kFdThreads, 0, stream>>>((const double2 *)H, N, start_ind, (const double2 *)data, psd,
-                                                    Fplus, Fcross, time_shift, df, B, nch, partial);
+    const double2 *H2 = (const double2 *)H, *d2 = (const double2 *)data;
+#define EOB_FD_LAUNCH(K)                                                                                         \
+    case K:                                                                                                      \
+        k_fd_split_lnl<K><<<grid, kFdThreads, 0, stream>>>(H2, N, start_ind, d2, ipsd, Fplus, Fcross, time_shift, \
+                                                           df, B, partial);                                      \
+        break;
+    switch (nch) {
+        EOB_FD_LAUNCH(1) EOB_FD_LAUNCH(2) EOB_FD_LAUNCH(3) EOB_FD_LAUNCH(4)
+        EOB_FD_LAUNCH(5) EOB_FD_LAUNCH(6) EOB_FD_LAUNCH(7) EOB_FD_LAUNCH(8)
+    }
+#undef EOB_FD_LAUNCH
     if (cudaGetLastError() != cudaSuccess) return EOB_E_CUDA;
     k_fd_finalize<<<blocks_for(B, 128), 128, 0, stream>>>(partial, nblk, B, df, lnl);
     return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;

@@ -282,7 +282,7 @@ int eob_detector_response(const double *ra, const double *dec, const double *psi
  * / psd_c(f) with data[c][N/2 + 1] (complex), psd[c][N/2 + 1], Fplus, Fcross,
  * time_shift[c * B + b] (the all_in_one_likelihood partials,
  * src/interpolate.cu:551-627, summed).  nch <= 8.  scratch: device memory of
- * eob_fd_lnl_scratch_bytes(B, N) bytes. */
+ * eob_fd_lnl_scratch_bytes(B, N) bytes (block partials and 1/psd). */
 size_t eob_fd_lnl_scratch_bytes(int B, int N);
 int eob_fd_lnl_from_fft(const double *H, int N, int start_ind, const double *data, const double *psd,
                         const double *Fplus, const double *Fcross, const double *time_shift, double df, int B, int nch,
