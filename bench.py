@@ -776,6 +776,9 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="integrator blocks (0: one wave of resident blocks)")
     ap.add_argument("--op", default=None, choices=["tdinterp2", "fd_lnl", "fd_split"],
                     help="time one kernel alone: mode synthesis TD2, FD likelihood partials, or the fused split-FFT FD likelihood")
+    ap.add_argument("--imr", action="store_true",
+                    help="attach NQC corrections and ringdowns (eob_options.imr, the drop-in class's default): "
+                         "the full inspiral-merger-ringdown template instead of the inspiral")
     ap.add_argument("--census", action="store_true",
                     help="FP64 census run: 128 copies of one binary through setup + integrator, 3 warm-up + 1 launch")
     args = ap.parse_args()
@@ -790,6 +793,18 @@ def main():
     if args.census:
         census(args)
         return
+    if args.imr:
+        # the oracle's likelihood (the accuracy sample, the CPU arms) is the
+        # inspiral template's; the completion's parity is checked against the
+        # oracle's own IMR restatement by tests/test_gpu_imr.py
+        args.accuracy_sample = 0
+        args.no_cpu_baseline = True
+        args.no_plain = True
+        args.no_serving = True
+        if args.impl != "native" or args.config not in (1, 2):
+            print(json.dumps({"impl": args.impl, "unavailable": "--imr is a native measurement on "
+                              "configurations 1 and 2 (the CPU arms time the inspiral template)"}))
+            return
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         line = run_reference(args, cfg, int(os.environ.get("WORLD_SIZE", "1")), rank)
@@ -825,6 +840,7 @@ def main():
     opt.grid = args.grid
     mixed = args.config in (3, 5) and not args.fp64
     opt.precision = 1 if mixed else 0
+    opt.imr = 1 if args.imr else 0
     P = torch.tensor(params, device=device)
     D = torch.tensor(data, device=device)
     order = longest_first(P)
@@ -976,7 +992,9 @@ def main():
         serving, _, _ = serving_measure(args, device, rank, ws, args.requests)
 
     graphed = chunked is None and not args.no_graph
-    extra_cfg = {"cuda_graph": graphed}
+    extra_cfg = {"cuda_graph": graphed,
+                 "template": "inspiral-merger-ringdown (NQC + ringdown attached on the GPU)" if args.imr
+                 else "inspiral (to the trajectory's last row)"}
     if chunked is not None:
         extra_cfg["chunks"] = chunked.info(B)
     if chunked is None and tuned is not None:

@@ -240,6 +240,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
     double om1 = 0.0, om2 = 0.0, om3 = 0.0, om4 = 0.0;
     int step = 0, first_row = 1, stage = 0, pass = 0, phase = kIdle, b = -1, st = 0;
     bool prevReject = false, fix = false;
+    bool nan_seen = false;  // this pass met a NaN error estimate (reported if the pass then fails)
     long long tries = 0;
     unsigned long long n_useful = 0, n_all = 0;  // RHS evaluations (census for the roofline)
     int n_bin = 0;                               // RHS evaluations of the current binary
@@ -390,6 +391,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             }
             errOld = 1e-4;
             prevReject = false;
+            nan_seen = false;
             tries = 0;
             first_row = step + 1;
             om1 = om2 = om3 = om4 = 0.0;
@@ -442,7 +444,18 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             }
             double denom = e1 + 0.01 * e2;
             denom = (denom < 0.0) ? 1.0 : denom;
-            const double err = fabs(h) * e1 * (0.5 * rsqrt(denom));  // |h| e1 sqrt(1 / (4 denom))
+            double err = fabs(h) * e1 * (0.5 * rsqrt(denom));  // |h| e1 sqrt(1 / (4 denom))
+            // A NaN error estimate -- a trial stage outside the Hamiltonian's
+            // domain, as when too long a step in the plunge carries a stage
+            // past the horizon -- counts as +inf: the attempt is rejected with
+            // the smallest scale.  (The reference's controller would carry
+            // the NaN into h, after which its integration cannot go on.)
+            // Tested on the bits: a comparison of doubles takes an FP64 slot.
+            const bool err_nan = ((unsigned long long)__double_as_longlong(err) << 1) > (0x7ff0000000000000ull << 1);
+            if (err_nan) {
+                err = __longlong_as_double(0x7ff0000000000000LL);
+                nan_seen = true;
+            }
             const double hOld = h;
             // controller (src/DOPR853.cu:674-762), beta = 0
             bool ok;
@@ -473,7 +486,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
             if (fix && !ok) hfix /= 2.0;
             if (fix) h = hfix;
             ++tries;
-            const bool bad = !(err == err) || !(h == h) || h == 0.0;
+            const bool bad = !(h == h) || h == 0.0;
             if (ok) {
                 for (int c = 0; c < NC; ++c) y[c] = ynew[c];
                 x = x + hOld;
@@ -490,7 +503,7 @@ __device__ __forceinline__ void integrate_body(const IntArgs &a, X *xch_all, uns
                 bool end = (step == first_row - 1);
                 if (end) st |= EOB_ST_STOP_REJECT;
                 if (bad) { st |= EOB_ST_NAN; end = true; }
-                if (tries >= a.max_tries) { st |= EOB_ST_TRIES; end = true; }
+                if (tries >= a.max_tries) { st |= EOB_ST_TRIES | (nan_seen ? EOB_ST_NAN : 0); end = true; }
                 if (!end) {
                     stage = 2;  // retry with the new h; k1 unchanged
                     if constexpr (kReg) {

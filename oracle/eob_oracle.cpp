@@ -404,7 +404,11 @@ double dopr_error(const double y[4], double hstep, double k[11][4], double ynew[
     }
     double denom = err + 0.01 * err2;
     denom = (denom < 0.0) ? 1.0 : denom;
-    return fabs(hstep) * err * sqrt(1.0 / (4.0 * denom));
+    const double e = fabs(hstep) * err * sqrt(1.0 / (4.0 * denom));
+    // a NaN estimate (a trial stage outside the Hamiltonian's domain) counts
+    // as +inf, a rejection with the smallest scale, as in the CUDA path; the
+    // reference's controller would carry the NaN into h
+    return (e != e) ? INFINITY : e;
 }
 
 // returns accept flag; updates h, errOld, prevReject
@@ -473,6 +477,7 @@ int integrate(const Binary &b, Dense &d, int step_num, double hInit, bool fix_st
     int stop_info = 0;
     std::vector<double> omegas((size_t)max_step, 0.0);
     double k[11][4];
+    long long tries = 0;  // attempt limit of the CUDA path (2 max_step + 100): every loop ends
     for (;;) {
         dopr_stages(b, y, h, k);
         double ynew[4];
@@ -490,7 +495,7 @@ int integrate(const Binary &b, Dense &d, int step_num, double hInit, bool fix_st
             stop_info = stop_code(b, y, step_num, omegas);
             stop = stop_info != 0;
         }
-        if (x >= tmax || step_num >= max_step - 1 || stop) break;
+        if (x >= tmax || step_num >= max_step - 1 || stop || ++tries >= 2LL * max_step + 100) break;
     }
     if (stop_out) *stop_out = stop_info;
     return step_num;
