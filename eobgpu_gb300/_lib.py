@@ -69,6 +69,7 @@ _SIGS = {
     "eob_ctx_ode": (c_int, [_P, _P, _P, _P, _P, c_int, _P, _P]),
     "eob_ctx_rr_force": (c_int, [_P, _P, _P, _P, _P, c_int, _P, _P]),
     "eob_ctx_root_find_scalar_all": (c_int, [_P, _P, _P, _P, _P, c_int, c_double, c_int, c_int, c_int, c_int, _P]),
+    "eob_ctx_compute_hlms": (c_int, [_P] * 11 + [c_int, _P, _P, c_int, c_int, _P, c_int, _P, _P]),
     "eob_ctx_waveform": (c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, c_int, c_int, _P, c_double, c_int, c_int,
                                  _P, _P]),
     "eob_dopr853_steps": (c_int, [_P] * 17 + [c_int, c_int, c_int, _P, _P, _P]),

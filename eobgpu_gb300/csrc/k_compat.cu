@@ -264,6 +264,42 @@ __global__ void k_ctx_waveform(const FacCoeffs *ctx, double *out, const double *
     out[2 * j + 1] = hl.im;
 }
 
+// compute_hlms (src/EOB.cu:3147-3322) as the function it was written to be:
+// one thread per (binary, trajectory row), every mode of the list.  H and
+// its gradients at the state and at p_r = 0 from the binary's additionalArgs
+// (as the reference's gradient calls), nu from m1_arr/m2_arr (as its
+// H_val), v = omega^(1/3), the vPhi input 1/(omega_c^2 r^3), the prefixes
+// [K][num_bin_all] that update_information was given.
+__global__ void k_ctx_compute_hlms(const FacCoeffs *ctx, double *hlms, const double *r_arr, const double *phi_arr,
+                                   const double *pr_arr, const double *L_arr, const double *m1_arr,
+                                   const double *m2_arr, const int *num_steps, int num_steps_max, const int *ells,
+                                   const int *mms, int K, int n, const double *add, const double *prefixes)
+{
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= (long long)n * num_steps_max) return;
+    const int b = (int)(j / num_steps_max), i = (int)(j % num_steps_max);
+    if (i >= num_steps[b]) return;
+    HamCoeffs h;
+    ham_of_add(&h, add, n, b);
+    const double r = r_arr[j], phi = phi_arr[j], pr = pr_arr[j], L = L_arr[j];
+    HamEval e;
+    ham_eval(h, r, pr, L, &e);
+    const double m1 = m1_arr[b], m2 = m2_arr[b];
+    const double nu = m1 * m2 / ((m1 + m2) * (m1 + m2));
+    const double Hval = nu * e.H;
+    const double v = cbrt(e.dHdL);
+    const double vPhi = 1.0 / (e.omega_c * e.omega_c * (r * r * r));
+    const double h22 = add[9 * (size_t)n + b];
+    for (int k = 0; k < K; ++k) {
+        const size_t pk = 2 * ((size_t)k * n + b);
+        const cdbl hl = mode_eval(ctx[b], ells[k], mms[k], prefixes[pk], prefixes[pk + 1], nu, r, phi, L, v, Hval,
+                                  vPhi, h22, false);
+        const size_t o = 2 * (((size_t)b * K + k) * num_steps_max + i);
+        hlms[o] = hl.re;
+        hlms[o + 1] = hl.im;
+    }
+}
+
 // ---- DOPR853 pieces (src/DOPR853.cu) ----
 __constant__ double kA[13][11];  // a[s][slot] (slot 1..10), zero where unused; filled by the host once
 __constant__ double kC[13];
@@ -576,6 +612,27 @@ int eob_ctx_waveform(const void *ctx, double *out, const double *r, const double
     k_ctx_waveform<<<nblk(n), kTPB, 0, stream>>>((const FacCoeffs *)ctx, out, r, phi, pphi, v, Hreal, eta, vPhiInput,
                                                   l, m, prefix, h22_calib, numSys, traj_length, idx);
     return ret(cudaGetLastError());
+}
+
+int eob_ctx_compute_hlms(const void *ctx, double *hlms, const double *r_arr, const double *phi_arr,
+                         const double *pr_arr, const double *L_arr, const double *m1_arr, const double *m2_arr,
+                         const double *chi1_arr, const double *chi2_arr, const int *num_steps, int num_steps_max,
+                         const int *ell_arr, const int *mm_arr, int num_modes, int num_bin_all,
+                         const double *additionalArgs, int num_add_args, const double *newtonian_prefixes,
+                         cudaStream_t stream)
+{
+    (void)chi1_arr;
+    (void)chi2_arr;
+    if (num_bin_all < 0 || num_steps_max < 0 || num_modes < 0) return EOB_E_ARG;
+    if (num_bin_all == 0 || num_steps_max == 0 || num_modes == 0) return EOB_OK;
+    if (!ctx || !hlms || !r_arr || !phi_arr || !pr_arr || !L_arr || !m1_arr || !m2_arr || !num_steps || !ell_arr ||
+        !mm_arr || !additionalArgs || !newtonian_prefixes || num_add_args < 10)
+        return EOB_E_ARG;
+    const long long total = (long long)num_bin_all * num_steps_max;
+    k_ctx_compute_hlms<<<nblk(total), kTPB, 0, stream>>>((const FacCoeffs *)ctx, hlms, r_arr, phi_arr, pr_arr, L_arr,
+                                                          m1_arr, m2_arr, num_steps, num_steps_max, ell_arr, mm_arr,
+                                                          num_modes, num_bin_all, additionalArgs, newtonian_prefixes);
+    return cudaGetLastError() == cudaSuccess ? EOB_OK : EOB_E_CUDA;
 }
 
 int eob_dopr853_steps(const double *x, double *xCurrent, const double *solOld, const double *h, double *arg,

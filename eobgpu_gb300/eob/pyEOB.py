@@ -135,5 +135,18 @@ class SEOBNRv5Class:
                                             addr(newtonian_prefix), float(h22_calib), int(numSys), int(traj_length),
                                             addr(hCoeffs_index), stream()), "EOBGetSpinFactorizedWaveform")
 
-    def compute_hlms(self, *args, **kwargs):
-        raise NotImplementedError("compute_hlms is dead code in the reference (src/EOB.cu:3147-3339, store disabled)")
+    def compute_hlms(self, hlms, r_arr, phi_arr, pr_arr, L_arr, m1_arr, m2_arr, chi1_arr, chi2_arr, num_steps,
+                     num_steps_max, ell_arr_in, mm_arr_in, num_modes, num_bin_all, additionalArgsIn, num_add_args):
+        """src/eob.pyx:178 -> eob_ctx_compute_hlms: the modes on the trajectory
+        rows, hlms[num_bin_all][num_modes][num_steps_max] (complex128), with the
+        Newtonian prefixes given to update_information.  The reference's kernel
+        never stores its result (src/EOB.cu:3319); this one does."""
+        self._need()
+        if self.newtonian_prefixes is None:
+            raise RuntimeError("compute_hlms needs the Newtonian prefixes given to update_information")
+        _lib.check(_lib_().eob_ctx_compute_hlms(addr(self._ctx), addr(hlms), addr(r_arr), addr(phi_arr),
+                                                addr(pr_arr), addr(L_arr), addr(m1_arr), addr(m2_arr),
+                                                addr(chi1_arr), addr(chi2_arr), addr(num_steps), int(num_steps_max),
+                                                addr(ell_arr_in), addr(mm_arr_in), int(num_modes), int(num_bin_all),
+                                                addr(additionalArgsIn), int(num_add_args),
+                                                addr(self.newtonian_prefixes), stream()), "compute_hlms")

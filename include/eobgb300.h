@@ -210,6 +210,26 @@ int eob_ctx_waveform(const void *ctx, double *out, const double *r, const double
                      const double *vPhiInput, int l, int m, const double *newtonian_prefix, double h22_calib,
                      int numSys, int traj_length, const int *hCoeffs_index, cudaStream_t stream);
 
+/* src/eob.pyx:178 SEOBNRv5Class.compute_hlms -> src/EOB.cu:3147-3322.  The
+ * reference's kernel computes the modes but never stores them (its store is
+ * commented out, :3319) and indexes its per-block shared arrays by trajectory
+ * row; this is the function it was written to be:
+ * hlms[(b num_modes + k) num_steps_max + i] (complex128) = h_lm, l = ell_arr[k],
+ * m = mm_arr[k] (device int arrays), of binary b at row i < num_steps[b] of
+ * r/phi/pr/L_arr [num_bin_all][num_steps_max], with H and its gradients at the
+ * state and at p_r = 0 from additionalArgs [num_add_args >= 10][num_bin_all]
+ * (rows m1, m2, chi1, chi2, omega0, K, d5, dSO, dSS, h22_calib), nu from m1/m2_arr,
+ * v = omega^(1/3), the vPhi input 1/(omega_c^2 r^3), ctx's coefficient tables
+ * and newtonian_prefixes [num_modes][num_bin_all] (complex128: the array
+ * update_information was given).  chi1/chi2_arr are accepted for the argument
+ * order and not read (additionalArgs carries the spins). */
+int eob_ctx_compute_hlms(const void *ctx, double *hlms, const double *r_arr, const double *phi_arr,
+                         const double *pr_arr, const double *L_arr, const double *m1_arr, const double *m2_arr,
+                         const double *chi1_arr, const double *chi2_arr, const int *num_steps, int num_steps_max,
+                         const int *ell_arr, const int *mm_arr, int num_modes, int num_bin_all,
+                         const double *additionalArgs, int num_add_args, const double *newtonian_prefixes,
+                         cudaStream_t stream);
+
 /* src/dopr853.pyx:67 dormandPrinceSteps -> src/DOPR853.cu:357 (one fused launch) */
 int eob_dopr853_steps(const double *x, double *xCurrent, const double *solOld, const double *h, double *arg,
                       const double *additionalArgs, double *k1, double *k2, double *k3, double *k4, double *k5,
