@@ -160,7 +160,9 @@ __global__ void __launch_bounds__(kSumThreads) k_fd_lnl(double2 *temp_sum, const
                     const double gr = fp * p.x + fc * c.x, gi = fp * p.y + fc * c.y;
                     const double rr = d.x - (gr * co + gi * s);
                     const double ri = d.y - (gi * co - gr * s);
-                    acc += (rr * rr + ri * ri) / psd[(size_t)ch * N + i];
+                    // reciprocal (seed + one Newton step, 3 FP64 instructions)
+                    // and a product instead of a division (about 6)
+                    acc = fma(fma(rr, rr, ri * ri), eob::eob_rcp(psd[(size_t)ch * N + i]), acc);
                 }
             }
 #pragma unroll
