@@ -91,3 +91,61 @@ def test_mirror_waveform_class_attaches_the_ringdown(golden, oracle):
             ref = md[q] / dist[b]
             assert np.max(np.abs(out[b, q, :n] - ref)) < 1e-8 * np.max(np.abs(ref)), (b, q)
             assert np.all(out[b, q, n:] == 0)
+
+
+def test_imr_ragged_batch_sample_vs_oracle(oracle):
+    """The completion on the ragged-batching population (M 20-200 Msun,
+    q 1-8, chi up to 0.9, f0 10-20 Hz, dt = 1/2048 s, N = 2^17): 16 binaries
+    spread over the 1024 of the benchmark's seeded draw, run as one batch,
+    against the oracle's restatement on the GPU's own knots, with the same IMR
+    length.  Bounds: the FP64 tolerances of configuration 1 (summed strain
+    within 1e-8 of its peak, phase at the peak within 1e-5 rad, lnL within 1e-9
+    relative), or twenty times the oracle's own one-ulp spread where that is
+    larger (tests/golden/imr_spread.npz: an ill-conditioned NQC system, with
+    coefficients up to ~1e7 that cancel, moves the corrected waveform by up to
+    ~1e-3 of its peak when its inputs move by one ulp)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import os
+    from eobgpu_gb300 import _lib, workload
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    from oracle import imr_oracle as imr
+    spread = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "imr_spread.npz"))
+    cfg = workload.CONFIGS[2]
+    params = workload.draw_params(cfg, stream=0)[::int(spread["stride"])]
+    np.testing.assert_array_equal(params, spread["params"])
+    N, dt = cfg.n_samples, cfg.dt
+    data = np.zeros(N)
+    o = _lib.default_options()
+    o.imr = 1
+    wl = WaveformLikelihood(len(params), 6000, [(2, 2)], N, options=o)
+    P = torch.tensor(params, device="cuda")
+    lnl, st = wl.run(P, torch.tensor(data, device="cuda"), dt, 1.0)
+    lnl, st = lnl.cpu().numpy(), st.cpu().numpy()
+    npts = wl.npts()
+    trajs = wl.trajectories()[3]
+    wl.prepare(P, dt)
+    hs, _ = wl.synth_strain(len(params), dt, N)
+    hs = hs.cpu().numpy()
+    assert np.all(st == 0), st
+    rows = []
+    for b in range(len(params)):
+        h, ll, info = imr.strain_and_lnl(oracle, params[b], dt, [(2, 2)], data, 1.0, replay_t=trajs[b][0])
+        n = int(info["npts_imr"])
+        assert npts[b] == n, (b, npts[b], n)
+        pk = np.max(np.abs(h))
+        k = int(np.argmax(np.abs(h)))
+        e = np.max(np.abs(hs[b, :n] - h[:n])) / pk
+        dphi = abs(np.angle(hs[b, k] / h[k]))
+        rel = abs(lnl[b] / ll - 1)
+        bs = max(1e-8, 20 * spread["strain"][b])
+        rows.append((b, e, dphi, rel, spread["strain"][b]))
+        assert e < bs, (b, params[b], e, bs)
+        assert dphi < max(1e-5, 20 * spread["strain"][b]), (b, dphi)
+        assert rel < max(1e-9, 20 * spread["lnl"][b]), (b, lnl[b], ll)
+    print("\nIMR ragged-batch sample, binary: strain of peak, dphi, rel lnL (oracle one-ulp strain spread)")
+    for b, e, dphi, rel, sp in rows:
+        print(f"  {b:2d}: {e:.2e} {dphi:.1e} {rel:.1e} ({sp:.1e})")
+    # the FP64 tolerances themselves hold for most of the sample
+    assert sum(1 for r in rows if r[1] < 1e-8 and r[3] < 1e-9) >= 12
