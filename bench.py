@@ -47,6 +47,9 @@ METRIC = "waveform+lnL evals/s"
 # need fewer instructions per right-hand side, so that roofline fractions
 # compare across versions.
 F_RHS = 1533.0
+# FP64 warp instructions per warp of a four-warp group per right-hand side
+# (profiles/k_integrate_quad_census.md): the work on the longest binary's chain
+QUAD_FP64_PER_WARP = 104.0
 
 TRAFFIC = os.path.join(ROOT, "profiles", "k_integrate_traffic_config2.md")
 
@@ -319,6 +322,28 @@ def run_reference(args, cfg, ws, rank):
                                        f"the reference's own code), one process per core"},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
+
+
+def longest_on_four_warps(args, B, nsm):
+    """Whether the launch puts the batch's longest binary on a four-warp group
+    (the automatic choice of the integrator's launcher, mirrored: lane groups
+    up to 32 while B * 2G <= nsm * 256, warp pairs up to B * 64 <= nsm * 512,
+    and with warp pairs a head of min(B / 64, 16) four-warp groups)."""
+    if args.lanes == 128:
+        return True
+    if args.head_quads == 0:
+        return False
+    G = args.lanes
+    if G not in (1, 2, 4, 8, 16, 32, 64):
+        target = nsm * 4 * 32 * 2
+        G = 1
+        while G < 32 and B * G * 2 <= target:
+            G *= 2
+        if G == 32 and B * 64 <= 2 * target:
+            G = 64
+    if args.head_quads > 0:
+        return G == 64 or 8 <= G <= 32
+    return G == 64 and B >= 64
 
 
 def config_block(cfg, args, extra=None):
@@ -962,6 +987,13 @@ def main():
                 # the chain's length in FP64 issue slots of one SM sub-partition
                 # (one FP64 warp instruction per 64 cycles at the sampled clock)
                 "fp64_slots_per_rhs_on_path": us_rhs * sm_mhz / 64.0}
+    if longest_on_four_warps(args, B, torch.cuda.get_device_properties(device).multi_processor_count) \
+            and chunked is None:
+        # the chain's own roofline: the FP64 instructions a warp of a four-warp
+        # group issues per right-hand side (ncu census of the four-warp kernel)
+        # against the slots the chain takes
+        critical["fp64_issue_frac_of_chain"] = QUAD_FP64_PER_WARP / critical["fp64_slots_per_rhs_on_path"]
+        critical["fp64_per_warp_per_rhs"] = QUAD_FP64_PER_WARP
     # FP64 peak of this device, measured
     fp64_peak = fp64_peak_tflops(wl.lib, device)
     roof = None
