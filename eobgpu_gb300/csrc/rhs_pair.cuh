@@ -178,8 +178,8 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         x.b[2][lane] = b.qa;
         x.b[3][lane] = b.qad;
         if (lane == 0) {
-            x.aux[0] = y[2] / y[3];
-            x.aux[1] = 1.0 / (8.0 * kPi * J.nu);
+            x.aux[0] = y[2] * eob_rcp(y[3]);
+            x.aux[1] = J.inv8pinu;
         }
         pair_sync(ps);  // 2
         const HeffPart o = comb_odd(J, jt, u, eob_rcp(jt[J_DC].v), pr, L);

@@ -188,7 +188,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     } else if (lane == 0) {
         // written after barrier 2 of this right-hand side, so no warp still
         // reads the previous value (it is read between barriers 5 and 6)
-        x.aux[0] = y[2] / y[3];
+        x.aux[0] = y[2] * eob_rcp(y[3]);
     }
     pair_sync(ps);  // 3: even and odd parts, s^2 and 1/s
 
