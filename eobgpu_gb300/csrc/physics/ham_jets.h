@@ -44,6 +44,7 @@ struct HamJets {
     double c[kNumJets][kJetTerms], l[kNumJets][kJetTerms], s[kNumJets][kJetTerms];
     double n4, apsq, nu, M;
     double inv8pinu;  // 1 / (8 pi nu): the flux's factor omega / (8 pi nu)
+    double inv_nu;    // 1 / nu: H = H_real / nu without a division
     // The log r and sqrt(u) polynomials have one or two adjacent terms per
     // jet: L = u^k (a + b u) with k = lk (3..5) and lc = {a, b, k a, (k+1) b};
     // S = s u^k with k = sk (2..6) and sc = {s, k s} (zero where a jet has no
@@ -124,6 +125,7 @@ EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
     J->nu = h.nu;
     J->M = h.M;
     J->inv8pinu = 1.0 / (8.0 * kPi * h.nu);
+    J->inv_nu = 1.0 / h.nu;
 }
 
 // powers of u for the sparse log r and sqrt(u) polynomials
@@ -387,7 +389,7 @@ EOB_HD HamPart comb_final(const HamJets &J, double u, const HeffPart &ev, const 
     const double s = s2 * rs;
     const double f = M * rs;
     HamPart o;
-    o.H = M * s / nu;
+    o.H = (M * s) * J.inv_nu;
     o.Hreal = M * s;
     o.dHdr = -(u * u) * f * (ev.du + od.du);
     o.dHdpr = f * (ev.dp + od.dp);
@@ -404,7 +406,7 @@ EOB_HD HamPart comb_final_s(const HamJets &J, double u, const HeffPart &ev, cons
     const double s = s2 * rs;
     const double f = M * rs;
     HamPart o;
-    o.H = M * s / nu;
+    o.H = (M * s) * J.inv_nu;
     o.Hreal = M * s;
     o.dHdr = -(u * u) * f * (ev.du + od.du);
     o.dHdpr = f * (ev.dp + od.dp);
