@@ -101,16 +101,31 @@ EOB_HD double eob_log_normal(int64_t bits)
     return hi + (lo + p);
 }
 
-EOB_HD double eob_log(double x)
+// arguments outside the normal positive range (NaN, negative, zero, +inf,
+// subnormal): kept out of line on the device, so that every inlined log
+// carries only the normal path (the kernels that inline it are large, and
+// their instruction fetch is part of the critical path)
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__
+#else
+inline
+#endif
+double eob_log_special(double x)
 {
     const int64_t bits = dbl_bits(x);
-    // normal, positive, finite: exponent field in [1, 2046], sign clear
-    if ((uint64_t)bits - 0x0010000000000000ULL < 0x7fe0000000000000ULL) return eob_log_normal(bits);
     if (x != x || x < 0.0) return bits_dbl(0x7ff8000000000000LL);  // NaN
     if (x == 0.0) return -bits_dbl(0x7ff0000000000000LL);           // -inf
     if (bits == 0x7ff0000000000000LL) return x;                      // +inf
     // subnormal: scale by 2^54
     return eob_log_normal(dbl_bits(x * 18014398509481984.0)) - 54.0 * EOB_LN2_HI - 54.0 * EOB_LN2_LO;
+}
+
+EOB_HD double eob_log(double x)
+{
+    const int64_t bits = dbl_bits(x);
+    // normal, positive, finite: exponent field in [1, 2046], sign clear
+    if ((uint64_t)bits - 0x0010000000000000ULL < 0x7fe0000000000000ULL) return eob_log_normal(bits);
+    return eob_log_special(x);
 }
 
 }  // namespace eob
