@@ -655,7 +655,11 @@ def serving_measure(args, device, rank, ws, n_requests, precision=1, plain_sampl
     max_steps = 4000
     _, data, amp = make_inputs(cfg, rank, device, max_steps)
     lanes = getattr(args, "lanes", 0) or 8
-    classes = [(1500, 1024, 2), (max_steps, 512, 1)]
+    # slot classes by trajectory capacity: four concurrent batches of up to
+    # 2048 short binaries and one of 1024 long ones (a sweep of batch sizes
+    # 1024..4096, 2..8 slots and 4..16 lanes per binary on the saturated
+    # trace put the capacity's plateau here)
+    classes = [(1500, 2048, 4), (max_steps, 1024, 1)]
     server = LikelihoodServer(data, cfg.dt, amp, classes=classes, lanes_per_binary=lanes, precision=precision,
                               head_quads=getattr(args, "head_quads", -1), device=device)
     trace = workload.serving_trace(n_requests, 1.0, stream=rank)
