@@ -33,8 +33,8 @@ struct WsLayout {
     size_t bins, fac, traj, nsteps, status, rhs, queue, row_off, chunk_off, npts, tin, ys, cA, cB, cC, cD, partial, f32,
         dataf, total;
     // merger-ringdown section (after everything else; present when imr): splines of r
-    // and p_r ([2][rows] each), attachment records, per-binary attachment, window scratch
-    size_t imr_ys, imr_cA, imr_cB, imr_cC, imr_cD, imr_rec, imr_bin, imr_scr, imr_total;
+    // and p_r ([2][rows] each), attachment records, per-binary attachment
+    size_t imr_ys, imr_cA, imr_cB, imr_cC, imr_cD, imr_rec, imr_bin, imr_total;
     int Bc, Lc, Kc, Nc, nsubs, max_chunks, imr;
 };
 
@@ -58,7 +58,6 @@ struct ImrBin {
 };
 
 constexpr int kImrWin = 256;  // longest fit window on the uniform grid [samples]
-constexpr int kImrScr = 9;    // scratch arrays of kImrWin doubles per (binary, mode)
 
 EOB_HD constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -100,7 +99,6 @@ EOB_HD constexpr WsLayout ws_layout(int Bc, int Lc, int Kc, int Nc, int imr = 0)
     w.imr_cD = o;    o = align256(o + sizeof(double) * rows * 2);
     w.imr_rec = o;   o = align256(o + sizeof(ImrRec) * (size_t)Bc * (size_t)Kc);
     w.imr_bin = o;   o = align256(o + sizeof(ImrBin) * (size_t)Bc);
-    w.imr_scr = o;   o = align256(o + sizeof(double) * kImrScr * kImrWin * (size_t)Bc * (size_t)Kc);
     w.imr_total = o;
     if (imr) w.total = o;
     return w;
@@ -125,7 +123,6 @@ struct Ws {
     double *imr_ys, *imr_cA, *imr_cB, *imr_cC, *imr_cD;  // series 0: r, 1: p_r
     ImrRec *imr_rec;                                     // [b * Kc + q]
     ImrBin *imr_bin;
-    double *imr_scr;
     WsLayout L;
 };
 
@@ -160,7 +157,6 @@ inline Ws ws_views(void *base, const WsLayout &L)
     w.imr_cD = imr ? (double *)(b + L.imr_cD) : nullptr;
     w.imr_rec = imr ? (ImrRec *)(b + L.imr_rec) : nullptr;
     w.imr_bin = imr ? (ImrBin *)(b + L.imr_bin) : nullptr;
-    w.imr_scr = imr ? (double *)(b + L.imr_scr) : nullptr;
     w.L = L;
     return w;
 }

@@ -1,7 +1,7 @@
 // Merger-ringdown attachment of the waveform (SEOBNRv4PHM.compute_full_waveform,
 // eob/seobnrv4phm.py:2374-2557), after the splines of the inspiral.
 //
-// One thread per (binary, mode).  On the uniform grid t_k = k dT + t0 of the
+// One warp per (binary, mode).  On the uniform grid t_k = k dT + t0 of the
 // binary's inspiral (k < npts):
 //   t_peak     knot of the largest orbital frequency (the phase spline's slope)
 //   attachment t_peak - Delta t_22 (NR fit); the (5,5) mode's NQC point 10 M earlier
@@ -16,7 +16,7 @@
 // A second kernel commits per binary: the IMR length (the inspiral to the
 // attachment sample, then 30 (2,2) damping times of ringdown) or, if a window
 // fell outside the waveform or exceeded kImrWin samples, the inspiral alone
-// with EOB_ST_IMR.  The windows live in the workspace's IMR section.
+// with EOB_ST_IMR.  The windows live in the block's shared memory.
 #include "eob_device.cuh"
 #include "physics/imr_fits.h"
 
@@ -139,21 +139,25 @@ __device__ __forceinline__ void nak_row(const double *t, const double *y, int n,
 // value, first and second derivative at te of the not-a-knot spline through
 // (t, y)[0..n), evaluated as CubicSplineInterpolantTD: interval
 // searchsorted(right) - 1, the last knot with its own degenerate row.
-// dg, bb: scratch of n doubles.
+// dg, bb: scratch of n doubles (the forward sweep's diagonal and right-hand
+// side, carried from row to row in registers and stored for the back
+// substitution).
 __device__ void window_spline(const double *t, const double *y, int n, double *dg, double *bb, double te,
                               double out[3])
 {
-    double a, b, c, d, cprev = 0.0;
+    double a, b, c, d, cprev = 0.0, dgp = 0.0, bbp = 0.0;
     for (int i = 0; i < n; ++i) {
         nak_row(t, y, n, i, &a, &b, &c, &d);
         if (i == 0) {
-            dg[0] = b;
-            bb[0] = d;
+            dgp = b;
+            bbp = d;
         } else {
-            const double wgt = a / dg[i - 1];
-            dg[i] = b - wgt * cprev;
-            bb[i] = d - wgt * bb[i - 1];
+            const double wgt = a / dgp;
+            dgp = b - wgt * cprev;
+            bbp = d - wgt * bbp;
         }
+        dg[i] = dgp;
+        bb[i] = bbp;
         cprev = c;
     }
     // interval of te
@@ -198,22 +202,32 @@ __device__ void window_spline(const double *t, const double *y, int n, double *d
     out[2] = 2 * c2 + 6 * c3 * xx;
 }
 
-// np.unwrap of angles a[0..n) in place (discontinuity pi)
-__device__ void unwrap(double *a, int n)
+// np.unwrap of angles a[0..n) in place (discontinuity pi) by one warp: each
+// lane forms the corrections of its samples from the original values (corr:
+// scratch of n doubles), then lane 0 accumulates them in order.  Adding a
+// zero correction leaves the running sum's bits unchanged (it starts at +0
+// and a sum of doubles is never -0 unless both terms are), so the result is
+// that of the serial loop.
+__device__ void unwrap_warp(double *a, double *corr, int n, int lane)
 {
     const double pi = kPi, two_pi = 2.0 * kPi;
-    double cum = 0.0, prev = a[0];
-    for (int i = 1; i < n; ++i) {
-        const double cur = a[i];
-        const double dd = cur - prev;
+    for (int i = 1 + lane; i < n; i += 32) {
+        const double dd = a[i] - a[i - 1];
         double dm = fmod(dd + pi, two_pi);
         if (dm < 0.0) dm += two_pi;
         dm -= pi;
         if (dm == -pi && dd > 0.0) dm = pi;
-        if (fabs(dd) >= pi) cum += dm - dd;
-        prev = cur;
-        a[i] = cur + cum;
+        corr[i] = (fabs(dd) >= pi) ? dm - dd : 0.0;
     }
+    __syncwarp();
+    if (lane == 0) {
+        double cum = 0.0;
+        for (int i = 1; i < n; ++i) {
+            cum += corr[i];
+            a[i] += cum;
+        }
+    }
+    __syncwarp();
 }
 
 // A x = y for 3x3 / 2x2 by elimination with partial pivoting (LAPACK gesv's method)
@@ -241,11 +255,26 @@ __device__ void solve_small(double A[N][N], double y[N], double x[N])
     }
 }
 
-__global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
+// Shared memory of one (binary, mode): the window's samples t, |h|, phase,
+// r, p_r, omega (arrays 0..5), the series of the NQC columns q_1..q_3 |h|,
+// p_1, p_2 (6..10) and the elimination scratch of the splines (11..21, then
+// r, p_r and omega once the series exist): 22 arrays of kImrWin doubles.
+constexpr int kImrArr = 22;
+// scratch array k = 0..13 of the splines (lane s: diagonal 2 s, right-hand side 2 s + 1)
+__device__ __forceinline__ int imr_scr_arr(int k) { return k < 11 ? 11 + k : k - 8; }
+
+// One warp per (binary, mode): the lanes evaluate the window samples side by
+// side, the seven NQC splines (three q columns, |h|, two p columns, the
+// phase) run on lanes 0..6 and the two ringdown splines on lanes 0..1, each
+// the same serial solve as before; the small solves and the fits are formed
+// by every lane alike from shuffled values.
+__global__ void __launch_bounds__(32) k_imr(Ws w, ImrArgs ia)
 {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= ia.B * ia.K) return;
-    const int b = tid / ia.K, q = tid % ia.K;
+    __shared__ double sm[kImrArr * kImrWin];
+    const int lane = threadIdx.x;
+    const int item = blockIdx.x;  // b * K + q
+    if (item >= ia.B * ia.K) return;
+    const int b = item / ia.K, q = item % ia.K;
     const int l = ia.ells[q], m = ia.mms[q];
     ImrBin &bin = w.imr_bin[b];
     const int np = w.npts[b];
@@ -263,21 +292,42 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
     const double chiS = 0.5 * (chi1 + chi2), chiA = 0.5 * (chi1 - chi2);
     const double eta = m1 * m2 / ((m1 + m2) * (m1 + m2));
     const bool is55 = (l == 5 && m == 5);
+    auto arr = [&](int k) { return sm + k * kImrWin; };
 
-    // t_peak: the knot with the largest slope of the phase spline (first of equals)
+    // t_peak: the knot with the largest slope of the phase spline, the first
+    // of equals (a running maximum from knot 0 with a strict comparison:
+    // NaN slopes never win, and a NaN at knot 0 keeps knot 0).  Each lane
+    // takes every 32nd knot; the lanes' bests are merged by (value, lowest
+    // knot), an order in which every lane ends with the same winner.
     int ip = 0;
-    double om_max = w.cA[g.base];
-    for (int i = 1; i < g.n; ++i) {
-        const double v = w.cA[g.base + i];
-        if (v > om_max) { om_max = v; ip = i; }
+    {
+        const double *om = w.cA + g.base;
+        double lv = 0.0;
+        int li = -1;
+        for (int i = lane; i < g.n; i += 32) {
+            const double v = om[i];
+            if (li < 0 ? (v == v) : (v > lv)) {
+                lv = v;
+                li = i;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, lv, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, li, off);
+            if (oi >= 0 && (li < 0 || ov > lv || (ov == lv && oi < li))) {
+                lv = ov;
+                li = oi;
+            }
+        }
+        const double v0 = om[0];
+        ip = (v0 == v0 && li >= 0) ? li : 0;
     }
     const double t_peak = g.x[ip];
     const double dt22 = nr_delta_t22(m1, m2, chi1, chi2);
     const int idx = grid_nearest(g, t_peak - dt22);
 
-    double *scr = w.imr_scr + (size_t)tid * kImrScr * kImrWin;
-    double *T = scr, *AMP = scr + kImrWin, *PH = scr + 2 * kImrWin, *R = scr + 3 * kImrWin, *PR = scr + 4 * kImrWin,
-           *OM = scr + 5 * kImrWin, *Y = scr + 6 * kImrWin, *DG = scr + 7 * kImrWin, *BB = scr + 8 * kImrWin;
+    double *T = arr(0), *AMP = arr(1), *PH = arr(2), *R = arr(3), *PR = arr(4), *OM = arr(5);
     ImrRec c;
 
     // ---- NQC coefficients
@@ -285,10 +335,10 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
     const int idn = grid_nearest(g, t_nr);
     const int lo = idn - 7, W = np - lo;
     if (lo < 0 || W < 3 || W > kImrWin) {
-        atomicOr(&bin.fail, 1);
+        if (lane == 0) atomicOr(&bin.fail, 1);
         return;
     }
-    for (int j = 0; j < W; ++j) {
+    for (int j = lane; j < W; j += 32) {
         const Sample s = eval_sample(w, g, lo + j, q, m);
         T[j] = grid_t(g, lo + j);
         AMP[j] = sqrt(s.hr * s.hr + s.hi * s.hi);
@@ -297,37 +347,44 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
         PR[j] = s.pr;
         OM[j] = s.om;
     }
-    unwrap(PH, W);
-    double Q[3][3], sv[3];
-    for (int col = 0; col < 3; ++col) {
-        for (int j = 0; j < W; ++j) {
-            const double rO = R[j] * OM[j];
-            double qv = PR[j] * PR[j] / (rO * rO);
-            if (col >= 1) qv = qv / R[j];
-            if (col == 2) qv = qv / sqrt(R[j]);
-            Y[j] = qv * AMP[j];
-        }
-        window_spline(T, Y, W, DG, BB, t_nr, sv);
-        for (int i = 0; i < 3; ++i) Q[i][col] = sv[i];
+    __syncwarp();
+    unwrap_warp(PH, arr(11), W, lane);
+    // the series of the amplitude columns q_1 |h|, q_2 |h|, q_3 |h| and of the
+    // phase columns p_1, p_2
+    for (int j = lane; j < W; j += 32) {
+        const double rO = R[j] * OM[j];
+        const double q1 = PR[j] * PR[j] / (rO * rO);
+        const double q2 = q1 / R[j];
+        const double q3 = q2 / sqrt(R[j]);
+        arr(6)[j] = q1 * AMP[j];
+        arr(7)[j] = q2 * AMP[j];
+        arr(8)[j] = q3 * AMP[j];
+        const double p1 = PR[j] / (R[j] * OM[j]);
+        arr(9)[j] = p1;
+        arr(10)[j] = p1 * PR[j] * PR[j];
     }
+    __syncwarp();
+    // lane 0..2: q columns, 3: |h|, 4..5: p columns, 6: phase
+    double so[3] = {0.0, 0.0, 0.0};
+    if (lane < 7) {
+        const double *Y = (lane < 3) ? arr(6 + lane) : (lane == 3) ? AMP : (lane < 6) ? arr(5 + lane) : PH;
+        window_spline(T, Y, W, arr(imr_scr_arr(2 * lane)), arr(imr_scr_arr(2 * lane + 1)), t_nr, so);
+    }
+    double Q[3][3];
+    for (int col = 0; col < 3; ++col)
+        for (int i = 0; i < 3; ++i) Q[i][col] = __shfl_sync(0xffffffffu, so[i], col);
     double av[3];
-    window_spline(T, AMP, W, DG, BB, t_nr, av);
+    for (int i = 0; i < 3; ++i) av[i] = __shfl_sync(0xffffffffu, so[i], 3);
     double ya[3] = {fabs(nr_peak_amp(l, m, m1, m2, chiS, chiA)) - av[0], nr_peak_adot(l, m, m1, m2, chiS, chiA) - av[1],
                     nr_peak_addot(l, m, m1, m2, chiS, chiA) - av[2]};
     double xa[3];
     solve_small<3>(Q, ya, xa);
     double P[2][2];
     for (int col = 0; col < 2; ++col) {
-        for (int j = 0; j < W; ++j) {
-            const double p1 = PR[j] / (R[j] * OM[j]);
-            Y[j] = col == 0 ? p1 : p1 * PR[j] * PR[j];
-        }
-        window_spline(T, Y, W, DG, BB, t_nr, sv);
-        P[0][col] = -sv[1];
-        P[1][col] = -sv[2];
+        P[0][col] = -__shfl_sync(0xffffffffu, so[1], 4 + col);
+        P[1][col] = -__shfl_sync(0xffffffffu, so[2], 4 + col);
     }
-    window_spline(T, PH, W, DG, BB, t_nr, sv);
-    double om = sv[1], omd = sv[2];
+    double om = __shfl_sync(0xffffffffu, so[1], 6), omd = __shfl_sync(0xffffffffu, so[2], 6);
     omd = (om * omd > 0.0) ? fabs(omd) : -fabs(omd);
     om = fabs(om);
     const double chi_n = chiS + chiA * (m1 - m2) / (m1 + m2) / (1.0 - 2.0 * eta);
@@ -341,10 +398,11 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
     const int nfit = (int)(20.0 / g.dT) + 1;
     const int lo2 = idx - nfit, W2 = np - lo2;
     if (lo2 < 0 || W2 < 3 || W2 > kImrWin) {
-        atomicOr(&bin.fail, 1);
+        if (lane == 0) atomicOr(&bin.fail, 1);
         return;
     }
-    for (int j = 0; j < W2; ++j) {
+    __syncwarp();  // every lane's spline is done before the samples overwrite t, |h| and the phase
+    for (int j = lane; j < W2; j += 32) {
         const Sample s = eval_sample(w, g, lo2 + j, q, m);
         double mag, ph;
         nqc_factor(c, s.r, s.pr, s.om, &mag, &ph);
@@ -355,12 +413,15 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
         AMP[j] = sqrt(hr * hr + hi * hi);
         PH[j] = atan2(hi, hr);
     }
-    unwrap(PH, W2);
+    __syncwarp();
+    unwrap_warp(PH, arr(11), W2, lane);
     const double t_match = grid_t(g, idx);
     const double tq = t_match - (is55 ? 10.0 : 0.0);
-    window_spline(T, AMP, W2, DG, BB, tq, av);
-    window_spline(T, PH, W2, DG, BB, tq, sv);
-    const double amp0 = av[0], damp0 = av[1], phi0 = sv[0], om0 = sv[1];
+    // lane 0: |h|, lane 1: the phase
+    double sr[3] = {0.0, 0.0, 0.0};
+    if (lane < 2) window_spline(T, lane == 0 ? AMP : PH, W2, arr(imr_scr_arr(2 * lane)), arr(imr_scr_arr(2 * lane + 1)), tq, sr);
+    const double amp0 = __shfl_sync(0xffffffffu, sr[0], 0), damp0 = __shfl_sync(0xffffffffu, sr[1], 0);
+    const double phi0 = __shfl_sync(0xffffffffu, sr[0], 1), om0 = __shfl_sync(0xffffffffu, sr[1], 1);
 
     // ---- remnant, QNM, ansatz coefficients
     const double Mf = final_mass_seobnrv4(m1, m2, chi1, chi2);
@@ -385,6 +446,7 @@ __global__ void __launch_bounds__(128) k_imr(Ws w, ImrArgs ia)
     c.d2f = d2f;
     c.phi_match = phi0;
     c.eta = eta;
+    if (lane != 0) return;
     w.imr_rec[(size_t)b * w.L.Kc + q] = c;
     if (q == 0) {
         // ringdown length: 30 damping times of the (2,2) QNM, truncated to whole M
@@ -429,8 +491,7 @@ cudaError_t launch_imr(const Ws &w, const RunArgs &a, cudaStream_t s)
     ia.K = a.K;
     for (int j = 0; j < kMaxModes; ++j) { ia.ells[j] = a.ells[j]; ia.mms[j] = a.mms[j]; }
     ia.dt = a.dt;
-    const int n = a.B * a.K;
-    k_imr<<<(n + 127) / 128, 128, 0, s>>>(w, ia);
+    k_imr<<<a.B * a.K, 32, 0, s>>>(w, ia);
     k_imr_commit<<<(a.B + 127) / 128, 128, 0, s>>>(w, a.B);
     return cudaGetLastError();
 }
