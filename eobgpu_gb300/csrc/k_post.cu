@@ -182,48 +182,6 @@ __global__ void __launch_bounds__(128) k_modes(Ws w, int B, ModeArgs ma)
     }
 }
 
-// Not-a-knot spline of n knots (src/interpolate.cu:10-267): Bv rhs -> slopes;
-// ud/dg/ld end up holding c1/c2/c3 on rows 0..n-2.
-__device__ void spline_one(const double *x, const double *y, int n, double *Bv, double *ud, double *dg, double *ld)
-{
-    for (int i = 0; i < n; ++i) {
-        int i0, i1, i2;
-        if (i == n - 1) { i0 = n - 3; i1 = n - 2; i2 = n - 1; }
-        else if (i == 0) { i0 = 0; i1 = 1; i2 = 2; }
-        else { i0 = i - 1; i1 = i; i2 = i + 1; }
-        const double x0 = x[i0], x1 = x[i1], x2 = x[i2];
-        const double dx1 = x1 - x0, dx2 = x2 - x1, d = x2 - x0;
-        const double y1 = y[i1];
-        const double s1 = (y1 - y[i0]) / dx1, s2 = (y[i2] - y1) / dx2;
-        if (i == n - 1) {
-            Bv[i] = (dx2 * dx2 * s1 + (2 * d + dx2) * dx1 * s2) / d;
-            dg[i] = dx1; ld[i] = d; ud[i] = 0.0;
-        } else if (i == 0) {
-            Bv[i] = ((dx1 + 2 * d) * dx2 * s1 + dx1 * dx1 * s2) / d;
-            ud[i] = d; ld[i] = 0.0; dg[i] = dx2;
-        } else {
-            Bv[i] = 3.0 * (dx2 * s1 + dx1 * s2);
-            dg[i] = 2 * (dx1 + dx2); ud[i] = dx1; ld[i] = dx2;
-        }
-    }
-    for (int i = 1; i < n; ++i) {
-        const double wgt = ld[i] / dg[i - 1];
-        dg[i] = dg[i] - wgt * ud[i - 1];
-        Bv[i] = Bv[i] - wgt * Bv[i - 1];
-    }
-    Bv[n - 1] = Bv[n - 1] / dg[n - 1];
-    for (int i = n - 2; i >= 0; --i) Bv[i] = (Bv[i] - ud[i] * Bv[i + 1]) / dg[i];
-    for (int i = 0; i < n - 1; ++i) {
-        const double dx = x[i + 1] - x[i];
-        const double slope = (y[i + 1] - y[i]) / dx;
-        const double bi = Bv[i];
-        const double t = (bi + Bv[i + 1] - 2 * slope) / dx;
-        ud[i] = bi;
-        dg[i] = (slope - bi) / dx - t;
-        ld[i] = t / dx;
-    }
-}
-
 // Row i of the not-a-knot slope system (src/interpolate.cu:10-120):
 // a x_{i-1} + b x_i + c x_{i+1} = d.
 __device__ __forceinline__ void spline_row(const double *x, const double *y, int n, int i, double *a, double *b,

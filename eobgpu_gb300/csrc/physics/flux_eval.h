@@ -749,12 +749,6 @@ __device__ double flux_sum_group(const FluxTable &t, double pphi, double omega, 
 }
 
 template <int G>
-__device__ double flux_eval_group(const FluxTable &t, double pphi, double omega, double Hreal, double omega_c, int sub)
-{
-    return flux_sum_group<G>(t, pphi, omega, Hreal, omega_c, sub) * omega * omega / (8.0 * kPi);
-}
-
-template <int G>
 __device__ void eob_rhs_group(const HamJets &h, const FluxTable &t, const double y[4], double k[4], int sub)
 {
     HamEval e;
