@@ -149,3 +149,49 @@ def test_imr_ragged_batch_sample_vs_oracle(oracle):
         print(f"  {b:2d}: {e:.2e} {dphi:.1e} {rel:.1e} ({sp:.1e})")
     # the FP64 tolerances themselves hold for most of the sample
     assert sum(1 for r in rows if r[1] < 1e-8 and r[3] < 1e-9) >= 12
+
+
+def test_imr_window_too_long_keeps_the_inspiral():
+    """A binary whose ringdown fit window (the 20 M before the attachment)
+    spans more than 256 samples of its grid -- 200 Msun at dt = 1/16384 s,
+    dT = 0.062 M, 323 samples -- keeps its inspiral and reports EOB_ST_IMR
+    (128), as the inspiral-only run of the same binary: same length, same
+    strain, same lnL.  In the same batch the completion still attaches for a
+    60 Msun binary (dT = 0.21 M), whose status, length and lnL are bitwise
+    those of a batch without the first binary."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from eobgpu_gb300 import _lib
+    from eobgpu_gb300.pipeline import WaveformLikelihood
+    dt, N = 1.0 / 16384.0, 1 << 14
+    bad = [100.0, 100.0, 0.2, -0.1, 20.0]
+    good = [36.0, 24.0, 0.1, 0.3, 20.0]
+    rng = np.random.default_rng(7)
+    D = torch.tensor(rng.standard_normal(N), device="cuda")
+
+    def run(rows, imr):
+        o = _lib.default_options()
+        o.imr = imr
+        o.lanes_per_binary = 64
+        wl = WaveformLikelihood(len(rows), 20000, [(2, 2)], N, options=o)
+        P = torch.tensor(rows, dtype=torch.float64, device="cuda")
+        lnl, st = wl.run(P, D, dt, 1.0)
+        lnl, st = lnl.cpu().numpy(), st.cpu().numpy()
+        npts = wl.npts()
+        wl.prepare(P, dt)
+        hs, _ = wl.synth_strain(len(rows), dt, N)
+        return lnl, st, npts, hs.cpu().numpy()
+
+    lnl_a, st_a, n_a, h_a = run([bad, good], 1)
+    lnl_b, st_b, n_b, h_b = run([good], 1)
+    lnl_c, st_c, n_c, h_c = run([bad], 0)
+    assert st_a[0] == 128, st_a
+    assert st_c[0] == 0 and st_a[1] == 0 and st_b[0] == 0, (st_a, st_b, st_c)
+    # the first binary: its inspiral, as without the completion
+    assert n_a[0] == n_c[0]
+    assert np.array_equal(h_a[0], h_c[0])
+    assert lnl_a[0] == lnl_c[0], (lnl_a[0], lnl_c[0])
+    # the second: completed, and unaffected by its neighbour
+    assert n_a[1] == n_b[0] and np.array_equal(h_a[1], h_b[0])
+    assert lnl_a[1] == lnl_b[0], (lnl_a[1], lnl_b[0])
