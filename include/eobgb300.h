@@ -73,7 +73,9 @@ void eob_options_default(eob_options *o);
  * likelihood, eob/seobnrv4phm.py:2628-2726, 636-721).
  * params[B][5] = (m1, m2 [Msun], chi1z, chi2z, f0 [Hz]); data[N];
  * lnl[B] = -1/2 sum_{k<N} (data_k - amp Re sum_lm h_lm(t_k))^2 with h = 0
- * past each binary's last sample; status[B] per-binary EOB_ST_* bits.
+ * past each binary's last sample; status[B] per-binary EOB_ST_* bits.  A
+ * binary left without a template (its trajectory failed: EOB_ST_SHORT with
+ * the reason's bit) gets lnl = NaN.
  * order[B] (may be NULL) is the order in which the persistent integrator
  * takes binaries from its queue.
  */
