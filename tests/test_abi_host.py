@@ -104,3 +104,53 @@ def test_chunk_size_for_budget(lib):
         assert chunk_size_for_budget(budget, 16000, 1, 1 << 20, 10 ** 6) == B
         assert chunk_size_for_budget(budget - 1, 16000, 1, 1 << 20, 10 ** 6) == B - 1
     assert chunk_size_for_budget(10, 16000, 1, 1 << 20, 100) == 0
+
+
+def test_invalid_arguments_are_refused_before_any_launch(lib):
+    """eob_waveform_lnl and the allocation-free entry point check every size,
+    pointer and mode before any CUDA call, so the refusals run on the host:
+    EOB_E_ARG (1), outputs untouched.  Host buffers stand in for device ones
+    (nothing is dereferenced)."""
+    import numpy as np
+    E_ARG = 1
+    mb, ms, mk, mn = 4, 100, 1, 64
+    wsb = lib.eob_workspace_bytes(mb, ms, mk, mn)
+    ws = np.zeros(16, dtype=np.uint8)
+    params = np.zeros((mb, 5))
+    data = np.zeros(mn)
+    lnl = np.full(mb, 7.0)
+    st = np.full(mb, 7, dtype=np.int32)
+    P = lambda a: a.ctypes.data if a is not None else None
+
+    def call(ws_=ws, wsb_=wsb, mb_=mb, ms_=ms, mk_=mk, mn_=mn, params_=params, B=2, ells=(2,), mms=(2,), dt=1e-3,
+             data_=data, N=mn, lnl_=lnl, opt=None):
+        e = np.ascontiguousarray(ells, dtype=np.int32)
+        m = np.ascontiguousarray(mms, dtype=np.int32)
+        return lib.eob_waveform_lnl(P(ws_), wsb_, mb_, ms_, mk_, mn_, P(params_), None, B, P(e), P(m), len(e), dt,
+                                    P(data_), N, 1.0, ctypes.byref(opt) if opt is not None else None, P(lnl_),
+                                    P(st), None)
+
+    imr = _lib.default_options()
+    imr.imr = 1
+    cases = {
+        "B = 0": dict(B=0), "B > max_batch": dict(B=mb + 1),
+        "no modes": dict(ells=(), mms=()), "K > max_modes": dict(ells=(2, 2), mms=(2, 1)),
+        "l > 8": dict(ells=(9,), mms=(1,)), "m > l": dict(ells=(2,), mms=(3,)), "m < 1": dict(ells=(2,), mms=(0,)),
+        "dt = 0": dict(dt=0.0), "dt NaN": dict(dt=float("nan")),
+        "N = 0": dict(N=0), "N > max_samples": dict(N=mn + 1),
+        "no workspace": dict(ws_=None), "workspace too small": dict(wsb_=wsb - 1),
+        "max_steps < 4": dict(ms_=3), "no params": dict(params_=None), "no data": dict(data_=None),
+        "no lnl": dict(lnl_=None), "imr without its section": dict(opt=imr),
+    }
+    for name, kw in cases.items():
+        assert call(**kw) == E_ARG, name
+    assert np.all(lnl == 7.0) and np.all(st == 7)
+    # the allocation-free entry point: at most 16 binaries, one mode, 8192 samples
+    na = lib.eob_waveform_lnl_noalloc
+    e = np.array([2], dtype=np.int32)
+    for B, K, N in ((17, 1, 64), (0, 1, 64), (2, 2, 64), (2, 1, 8193), (2, 1, 0)):
+        pp = np.zeros((max(B, 1), 5))
+        ee = np.repeat(e, max(K, 1))
+        out = np.full(max(B, 1), 7.0)
+        assert na(P(pp), B, P(ee), P(ee), K, 1e-3, P(np.zeros(max(N, 1))), N, 1.0, None, P(out), P(st), None) == E_ARG
+        assert np.all(out == 7.0)
