@@ -513,7 +513,10 @@ EOB_HD bool table_flag(double x)
 #endif
 }
 
-// lm: lm_packed(i), passed by callers that keep it in a register
+// lm: lm_packed(i), passed by callers that keep it in a register; LMAX: an
+// upper bound on l of the multipoles evaluated together (the powers of rho
+// above it are not formed)
+template <int LMAX = kLMax>
 EOB_HD double flux_mode_s_rho_lm(const FluxTable &t, int i, int lm, const FluxLane &f, double rho)
 {
     const int l = lm >> 4, m = lm & 15;
@@ -521,10 +524,10 @@ EOB_HD double flux_mode_s_rho_lm(const FluxTable &t, int i, int lm, const FluxLa
     rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
     // rho^l by squaring (l = 2..8)
     const double r2 = rho * rho, r4 = r2 * r2;
-    double rpl = (l & 4) ? r4 : 1.0;
+    double rpl = (LMAX >= 4 && (l & 4)) ? r4 : 1.0;
     if (l & 2) rpl *= r2;
     if (l & 1) rpl *= rho;
-    if (l == 8) rpl = r4 * r4;
+    if (LMAX >= 8 && l == 8) rpl = r4 * r4;
     const double aux = f.v * fma(t.f3[i], f.v2, t.f1[i]);
     rpl = ((m & 1) && table_flag(t.equal_mass)) ? aux : rpl + aux;
     const double S2 = eps ? f.S2o : f.S2e;
@@ -537,7 +540,7 @@ EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, doub
 }
 
 // elm = eulerlog_m(v) = elog[m] + log v, passed by callers that form it once per m
-template <int KMAX>
+template <int KMAX, int LMAX = kLMax>
 EOB_HD double flux_mode_s_e(const FluxTable &t, int i, int lm, double elm, const FluxLane &f)
 {
     // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
@@ -549,19 +552,19 @@ EOB_HD double flux_mode_s_e(const FluxTable &t, int i, int lm, double elm, const
         if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
         acc = fma(acc, f.v, ck);
     }
-    return flux_mode_s_rho_lm(t, i, lm, f, fma(acc, f.v, 1.0));
+    return flux_mode_s_rho_lm<LMAX>(t, i, lm, f, fma(acc, f.v, 1.0));
 }
 
-template <int KMAX>
+template <int KMAX, int LMAX = kLMax>
 EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &f)
 {
-    return flux_mode_s_e<KMAX>(t, i, lm, t.elog[lm & 15] + f.lv, f);
+    return flux_mode_s_e<KMAX, LMAX>(t, i, lm, t.elog[lm & 15] + f.lv, f);
 }
 
-template <int KMAX>
+template <int KMAX, int LMAX = kLMax>
 EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
 {
-    return flux_mode_s_lm<KMAX>(t, i, lm_packed(i), f);
+    return flux_mode_s_lm<KMAX, LMAX>(t, i, lm_packed(i), f);
 }
 
 // rho_lm's series (degree <= 10) in two halves for two lanes: half 0 gives
@@ -594,10 +597,10 @@ EOB_HD double flux_mode_vp(int i, const FluxLane &f)
     return vpw;
 }
 
-template <int KMAX>
+template <int KMAX, int LMAX = kLMax>
 EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
 {
-    return flux_mode_s<KMAX>(t, i, f) * flux_mode_vp(i, f);
+    return flux_mode_s<KMAX, LMAX>(t, i, f) * flux_mode_vp(i, f);
 }
 
 // vphi^(2 (l + eps)) of multipole i from vphi^2 by squaring (l + eps = 2..9)
@@ -636,7 +639,7 @@ EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
 template <int KMAX, int LD = kLMax>
 EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
 {
-    return flux_mode_b<LD>(t, i, T, k4) * flux_mode_a<KMAX>(t, i, f);
+    return flux_mode_b<LD>(t, i, T, k4) * flux_mode_a<KMAX, LD>(t, i, f);
 }
 
 // Sequential use of the lane-group pieces (host tests)
