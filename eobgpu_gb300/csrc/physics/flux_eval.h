@@ -513,23 +513,31 @@ EOB_HD bool table_flag(double x)
 #endif
 }
 
-// lm: lm_packed(i), passed by callers that keep it in a register; LMAX: an
-// upper bound on l of the multipoles evaluated together (the powers of rho
-// above it are not formed)
-template <int LMAX = kLMax>
+// lm: lm_packed(i), passed by callers that keep it in a register.  LMAX,
+// LMIN: bounds on l of the multipoles evaluated together, so that what no
+// multipole in that range needs is not formed: the powers of rho above
+// LMAX; the h22 calibration term (the (2,2) multipole only) when LMIN > 2;
+// and f_lm = f1 v + f3 v^3 when LMIN > 4 (it is zero from l = 5 on,
+// flux_keeps_f), where rho^l + 0 is rho^l and f_lm alone (odd m at equal
+// mass) is 0
+template <int LMAX = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_s_rho_lm(const FluxTable &t, int i, int lm, const FluxLane &f, double rho)
 {
     const int l = lm >> 4, m = lm & 15;
     const int eps = (l + m) & 1;
-    rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
+    if constexpr (LMIN <= 2) rho = fma((i == lm_index(2, 2)) ? t.h22calib : 0.0, f.v12, rho);
     // rho^l by squaring (l = 2..8)
     const double r2 = rho * rho, r4 = r2 * r2;
     double rpl = (LMAX >= 4 && (l & 4)) ? r4 : 1.0;
     if (l & 2) rpl *= r2;
     if (l & 1) rpl *= rho;
     if (LMAX >= 8 && l == 8) rpl = r4 * r4;
-    const double aux = f.v * fma(t.f3[i], f.v2, t.f1[i]);
-    rpl = ((m & 1) && table_flag(t.equal_mass)) ? aux : rpl + aux;
+    if constexpr (LMIN <= 4) {
+        const double aux = f.v * fma(t.f3[i], f.v2, t.f1[i]);
+        rpl = ((m & 1) && table_flag(t.equal_mass)) ? aux : rpl + aux;
+    } else {
+        rpl = ((m & 1) && table_flag(t.equal_mass)) ? 0.0 : rpl;
+    }
     const double S2 = eps ? f.S2o : f.S2e;
     return S2 * (rpl * rpl);
 }
@@ -540,7 +548,7 @@ EOB_HD double flux_mode_s_rho(const FluxTable &t, int i, const FluxLane &f, doub
 }
 
 // elm = eulerlog_m(v) = elog[m] + log v, passed by callers that form it once per m
-template <int KMAX, int LMAX = kLMax>
+template <int KMAX, int LMAX = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_s_e(const FluxTable &t, int i, int lm, double elm, const FluxLane &f)
 {
     // rho = 1 + v (c1 + v (c2 + ... + v cK)), c_k = rho_k + rhol_k eulerlog_m
@@ -552,19 +560,19 @@ EOB_HD double flux_mode_s_e(const FluxTable &t, int i, int lm, double elm, const
         if (k == 6 || k == 7 || k == 8 || k == 10) ck = fma(t.rhol[i][k], elm, ck);
         acc = fma(acc, f.v, ck);
     }
-    return flux_mode_s_rho_lm<LMAX>(t, i, lm, f, fma(acc, f.v, 1.0));
+    return flux_mode_s_rho_lm<LMAX, LMIN>(t, i, lm, f, fma(acc, f.v, 1.0));
 }
 
-template <int KMAX, int LMAX = kLMax>
+template <int KMAX, int LMAX = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_s_lm(const FluxTable &t, int i, int lm, const FluxLane &f)
 {
-    return flux_mode_s_e<KMAX, LMAX>(t, i, lm, t.elog[lm & 15] + f.lv, f);
+    return flux_mode_s_e<KMAX, LMAX, LMIN>(t, i, lm, t.elog[lm & 15] + f.lv, f);
 }
 
-template <int KMAX, int LMAX = kLMax>
+template <int KMAX, int LMAX = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_s(const FluxTable &t, int i, const FluxLane &f)
 {
-    return flux_mode_s_lm<KMAX, LMAX>(t, i, lm_packed(i), f);
+    return flux_mode_s_lm<KMAX, LMAX, LMIN>(t, i, lm_packed(i), f);
 }
 
 // rho_lm's series (degree <= 10) in two halves for two lanes: half 0 gives
@@ -597,10 +605,10 @@ EOB_HD double flux_mode_vp(int i, const FluxLane &f)
     return vpw;
 }
 
-template <int KMAX, int LMAX = kLMax>
+template <int KMAX, int LMAX = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_a(const FluxTable &t, int i, const FluxLane &f)
 {
-    return flux_mode_s<KMAX, LMAX>(t, i, f) * flux_mode_vp(i, f);
+    return flux_mode_s<KMAX, LMAX, LMIN>(t, i, f) * flux_mode_vp(i, f);
 }
 
 // vphi^(2 (l + eps)) of multipole i from vphi^2 by squaring (l + eps = 2..9)
@@ -636,10 +644,10 @@ EOB_HD double flux_mode_b(const FluxTable &t, int i, double T, double k4)
     return flux_mode_b_l<LD>(t, i, lm_packed(i) >> 4, T, k4);
 }
 
-template <int KMAX, int LD = kLMax>
+template <int KMAX, int LD = kLMax, int LMIN = 2>
 EOB_HD double flux_mode_lane(const FluxTable &t, int i, const FluxLane &f, double T, double k4)
 {
-    return flux_mode_b<LD>(t, i, T, k4) * flux_mode_a<KMAX, LD>(t, i, f);
+    return flux_mode_b<LD>(t, i, T, k4) * flux_mode_a<KMAX, LD, LMIN>(t, i, f);
 }
 
 // Sequential use of the lane-group pieces (host tests)
@@ -705,6 +713,14 @@ EOB_HD constexpr int flux_lmax(int first, int n)
     return m;
 }
 
+// the smallest l among positions [first, first + n)
+EOB_HD constexpr int flux_lmin(int first, int n)
+{
+    int m = kLMax;
+    for (int p = first; p < first + n && p < kNumLM; ++p) m = kFluxLSorted[p] < m ? kFluxLSorted[p] : m;
+    return m;
+}
+
 template <int G, int R>
 __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const FluxLane &f, double Tm, double k4m,
                                                    int sub)
@@ -715,13 +731,14 @@ __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const Flu
     } else {
         constexpr int KM = kFluxDegSorted[first];
         constexpr int LD = flux_lmax(first, G);
+        constexpr int LN = flux_lmin(first, G);
         const int pos = first + sub;
         const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
         const int m = lm_packed(i) & 15;
         // the m factors live on lanes m-1 of the group
         const double T = __shfl_sync(0xffffffffu, Tm, m - 1, G);
         const double k4 = __shfl_sync(0xffffffffu, k4m, m - 1, G);
-        double here = flux_mode_lane<KM, LD>(t, i, f, T, k4);
+        double here = flux_mode_lane<KM, LD, LN>(t, i, f, T, k4);
         if (pos >= kNumLM) here = 0.0;
         return here + flux_rounds_lane<G, R + 1>(t, f, Tm, k4m, sub);
     }

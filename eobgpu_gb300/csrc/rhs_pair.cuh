@@ -115,7 +115,8 @@ __device__ __forceinline__ double flux_warp_modes(const FluxTable &t, const Flux
     const int pos = FIRST + lane;
     const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
     const int m = lm_packed(i) & 15;
-    const double here = flux_mode_lane<KM>(t, i, f, x.T[m - 1], x.k4[m - 1]);
+    const double here =
+        flux_mode_lane<KM, flux_lmax(FIRST, 32), flux_lmin(FIRST, 32)>(t, i, f, x.T[m - 1], x.k4[m - 1]);
     return (pos < kNumLM) ? here : 0.0;
 }
 

@@ -275,12 +275,13 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const double hv = flux_rho_half_e(t, ql.i, x.elm[(ql.lm & 15) - 1], f, lane >> 4);
         const double hi = __shfl_xor_sync(0xffffffffu, hv, 16);
         const double rho = fma(fma(x.fl[6], hi, hv), f.v, 1.0);
-        const double a_part = flux_mode_s_rho_lm<flux_lmax(0, 16)>(t, ql.i, ql.lm, f, rho);
+        const double a_part = flux_mode_s_rho_lm<flux_lmax(0, 16), flux_lmin(0, 16)>(t, ql.i, ql.lm, f, rho);
         if (lane < 16) x.a[lane] = a_part;
     } else if (q == 2) {
         // positions 16..34 (degree 4 .. 2)
         const int pos = 16 + lane;
-        const double a_part = flux_mode_s_e<kFluxDegSorted[16]>(t, ql.i, ql.lm, x.elm[(ql.lm & 15) - 1], f);
+        const double a_part = flux_mode_s_e<kFluxDegSorted[16], kLMax, flux_lmin(16, kNumLM - 16)>(
+            t, ql.i, ql.lm, x.elm[(ql.lm & 15) - 1], f);
         if (pos < kNumLM) x.a[pos] = a_part;
     } else {
         const int pos = (q == 1) ? lane : 32 + lane;
