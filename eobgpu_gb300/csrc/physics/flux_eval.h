@@ -404,8 +404,10 @@ EOB_HD double flux_mode_generic(const FluxTable &t, int i, const FluxShared &s, 
 // Multipole evaluation for lane groups of 8 or more lanes.  The factors that
 // depend on m only are computed once per call on lanes 0..7 of the group (one
 // exp(-m x) and one division per lane, in one instruction stream) and read by
-// shuffles; the Gamma product prod_{j<=l} (4 k^2 + j^2) is a polynomial in
-// 4 k^2 from a table; powers of v_phi^2 are precomputed and selected.
+// shuffles, the Gamma products prod_{j<=l} (4 k^2 + j^2) of every l among
+// them (a running product on lane m - 1); powers of v_phi^2 are precomputed
+// and selected.  (The warp pair and the four-warp group evaluate the Gamma
+// product as a polynomial in 4 k^2 from a table, flux_mode_b_l.)
 
 
 // per-call pieces shared by every multipole of one lane group
@@ -721,9 +723,11 @@ EOB_HD constexpr int flux_lmin(int first, int n)
     return m;
 }
 
+// gp: on lane m - 1 of the group, prod_{j<=l} (4 k^2 + j^2) of that m for
+// l = 2..8 (gp[l - 2]); each round reads only the l of its own range
 template <int G, int R>
-__device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const FluxLane &f, double Tm, double k4m,
-                                                   int sub)
+__device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const FluxLane &f, double Tm,
+                                                   const double (&gp)[kLMax - 1], int sub)
 {
     constexpr int first = R * G;
     if constexpr (first >= kNumLM) {
@@ -734,13 +738,18 @@ __device__ __forceinline__ double flux_rounds_lane(const FluxTable &t, const Flu
         constexpr int LN = flux_lmin(first, G);
         const int pos = first + sub;
         const int i = kFluxOrder[pos < kNumLM ? pos : kNumLM - 1];
-        const int m = lm_packed(i) & 15;
+        const int lm = lm_packed(i), l = lm >> 4, m = lm & 15;
         // the m factors live on lanes m-1 of the group
         const double T = __shfl_sync(0xffffffffu, Tm, m - 1, G);
-        const double k4 = __shfl_sync(0xffffffffu, k4m, m - 1, G);
-        double here = flux_mode_lane<KM, LD, LN>(t, i, f, T, k4);
+        double P = 0.0;
+#pragma unroll
+        for (int q = LN; q <= LD; ++q) {
+            const double pq = __shfl_sync(0xffffffffu, gp[q - 2], m - 1, G);
+            P = (l == q) ? pq : P;
+        }
+        double here = (t.gmul[i] * T * P) * flux_mode_a<KM, LD, LN>(t, i, f);
         if (pos >= kNumLM) here = 0.0;
-        return here + flux_rounds_lane<G, R + 1>(t, f, Tm, k4m, sub);
+        return here + flux_rounds_lane<G, R + 1>(t, f, Tm, gp, sub);
     }
 }
 
@@ -758,7 +767,17 @@ __device__ double flux_sum_group(const FluxTable &t, double pphi, double omega, 
         const FluxLane f = flux_lane_make_rv(t, pphi, omega, Hreal, v, vphi, eob_log(v));
         double Tm, k4m;
         flux_m_factors((sub & 7) + 1, 4.0 * kPi * Hreal * omega, Hreal * omega, &Tm, &k4m);
-        part = flux_rounds_lane<G, 0>(t, f, Tm, k4m, sub);
+        // the Gamma products of this lane's m for every l, by a running
+        // product (an add and a multiply per l) instead of a Horner sum of
+        // degree l in every round
+        double gp[kLMax - 1];
+        double p = k4m + 1.0;
+#pragma unroll
+        for (int l = 2; l <= kLMax; ++l) {
+            p *= k4m + (double)(l * l);
+            gp[l - 2] = p;
+        }
+        part = flux_rounds_lane<G, 0>(t, f, Tm, gp, sub);
     } else {
         const FluxShared s = flux_shared_make_rv(t, pphi, omega, Hreal, v, vphi);
         part = flux_rounds<G, 0>(t, s, Hreal * omega, sub);
