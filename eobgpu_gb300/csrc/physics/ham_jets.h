@@ -45,6 +45,7 @@ struct HamJets {
     double n4, apsq, nu, M;
     double inv8pinu;  // 1 / (8 pi nu): the flux's factor omega / (8 pi nu)
     double inv_nu;    // 1 / nu: H = H_real / nu without a division
+    double two_nu;    // 2 nu (exact): s^2 = 1 + 2 nu (H_eff - 1)
     // The log r and sqrt(u) polynomials have one or two adjacent terms per
     // jet: L = u^k (a + b u) with k = lk (3..5) and lc = {a, b, k a, (k+1) b};
     // S = s u^k with k = sk (2..6) and sc = {s, k s} (zero where a jet has no
@@ -126,6 +127,7 @@ EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
     J->M = h.M;
     J->inv8pinu = 1.0 / (8.0 * kPi * h.nu);
     J->inv_nu = 1.0 / h.nu;
+    J->two_nu = 2.0 * h.nu;
 }
 
 // powers of u for the sparse log r and sqrt(u) polynomials
@@ -369,7 +371,7 @@ EOB_HD HeffPart comb_odd_parts(const Jet *jt, double u, double idc, const PartN 
     HeffPart o;
     o.v = L * u3i * n.Nv;
     o.du = L * idc * (3.0 * u2 * n.Nv + u3 * n.Nu - u3 * n.Nv * idc * dc.d);
-    o.dp = L * u3i * n.Np * 2.0 * pr;
+    o.dp = (L * u3i * n.Np) * (2.0 * pr);  // the same bits: both products by 2 are exact
     o.dL = u3i * n.Nv;
     return o;
 }
@@ -383,8 +385,8 @@ EOB_HD HeffPart comb_odd(const HamJets &J, const Jet *jt, double u, double idc, 
 EOB_HD HamPart comb_final(const HamJets &J, double u, const HeffPart &ev, const HeffPart &od)
 {
     const double heff = ev.v + od.v;
-    const double nu = J.nu, M = J.M;
-    const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
+    const double M = J.M;
+    const double s2 = fma(J.two_nu, heff - 1.0, 1.0);
     const double rs = eob_rsqrt(s2);
     const double s = s2 * rs;
     const double f = M * rs;

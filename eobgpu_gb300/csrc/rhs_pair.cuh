@@ -243,7 +243,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         // log v = log(omega) / 3, here rather than after the cube root on the
         // other warp, whose flux set-up is the longer of the two
         const double heff = x.ev[0][0] + x.od[0][0];
-        const double s2 = fma(2.0 * J.nu, heff - 1.0, 1.0);
+        const double s2 = fma(J.two_nu, heff - 1.0, 1.0);
         const double omega = (J.M * D) * eob_rsqrt(s2);
         const double lv = eob_log(omega) * (1.0 / 3.0);
         if (lane == 0) x.fl[1] = lv;

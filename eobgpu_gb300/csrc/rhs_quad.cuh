@@ -182,7 +182,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         const double AW = x.pa[0][lane] * W;
         const double u3i = u3 * x.idc[lane];
         const double od = L * u3i * x.pn[0][lane];
-        const double s2 = fma(2.0 * J.nu, fma(AW, eob_rsqrt(AW), od) - 1.0, 1.0);
+        const double s2 = fma(J.two_nu, fma(AW, eob_rsqrt(AW), od) - 1.0, 1.0);
         x.hs[0][lane] = s2;
         x.hs[1][lane] = eob_rsqrt(s2);
     } else if (lane == 0) {
