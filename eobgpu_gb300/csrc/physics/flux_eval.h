@@ -29,6 +29,7 @@ struct FluxTable {
     double elog[kLMax + 1];   // gamma + log(2 m), m = 1..8: eulerlog_m(v) = elog[m] + log v
     double gmul[kNumLM];      // m^2 nabs2 / (l!)^2 (lane-group evaluator)
     double inv2eta;           // 1 / (2 eta) (lane-group evaluator)
+    double fo_scale;          // inv2eta / (4 pi): F / omega = S omega fo_scale
 
     EOB_HD double c_rho(int i, int k) const { return rho[i][k]; }
     EOB_HD double c_rhol(int i, int k) const { return rhol[i][k]; }
@@ -41,6 +42,7 @@ struct FluxTable {
     EOB_HD double c_h22() const { return h22calib; }
     EOB_HD double c_gmul(int i, int, int) const { return gmul[i]; }
     EOB_HD double c_inv2eta() const { return inv2eta; }
+    EOB_HD double c_fo_scale() const { return fo_scale; }
 };
 
 // The same flux inputs read straight from a FacCoeffs table and
@@ -73,6 +75,7 @@ struct FacFluxView {
         return (double)(m * m) * c_nabs2(i, l, m) / (f * f);
     }
     EOB_HD double c_inv2eta() const { return 0.5 / eta; }
+    EOB_HD double c_fo_scale() const { return c_inv2eta() * (0.25 / kPi); }
 };
 
 EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *prefix_re, const double *prefix_im,
@@ -100,6 +103,7 @@ EOB_HD void flux_table_build(FluxTable *t, const FacCoeffs &fc, const double *pr
     if (eta > 0.25 && eta < 0.25 + 1e-4) eta = 0.25;
     t->eta = eta;
     t->inv2eta = 0.5 / eta;
+    t->fo_scale = t->inv2eta * (0.25 / kPi);
     t->equal_mass = (eta == 0.25) ? 1.0 : 0.0;
     t->elog[0] = 0.0;
     for (int m = 1; m <= kLMax; ++m) t->elog[m] = kEulerGamma + log(2.0 * m);
@@ -296,7 +300,7 @@ EOB_HD double flux_eval(const Tab &t, double r, double pphi, double omega, doubl
 template <class Tab>
 EOB_HD double flux_over_omega(const Tab &t, double S, double omega)
 {
-    return (S * omega) * (t.c_inv2eta() * (0.25 / kPi));
+    return (S * omega) * t.c_fo_scale();
 }
 
 // ODE right-hand side (src/EOB.cu:3046-3145): k = (dH/dpr, dH/dpphi,

@@ -46,6 +46,7 @@ struct HamJets {
     double inv8pinu;  // 1 / (8 pi nu): the flux's factor omega / (8 pi nu)
     double inv_nu;    // 1 / nu: H = H_real / nu without a division
     double two_nu;    // 2 nu (exact): s^2 = 1 + 2 nu (H_eff - 1)
+    double M2;        // M^2 (the same product the right-hand sides formed per call)
     // The log r and sqrt(u) polynomials have one or two adjacent terms per
     // jet: L = u^k (a + b u) with k = lk (3..5) and lc = {a, b, k a, (k+1) b};
     // S = s u^k with k = sk (2..6) and sc = {s, k s} (zero where a jet has no
@@ -128,6 +129,7 @@ EOB_HD void ham_jets_build(const HamCoeffs &h, HamJets *J)
     J->inv8pinu = 1.0 / (8.0 * kPi * h.nu);
     J->inv_nu = 1.0 / h.nu;
     J->two_nu = 2.0 * h.nu;
+    J->M2 = h.M * h.M;
 }
 
 // powers of u for the sparse log r and sqrt(u) polynomials

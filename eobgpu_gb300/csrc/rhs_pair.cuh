@@ -233,7 +233,7 @@ __device__ __forceinline__ void eob_rhs_pair(const HamJets &J, const FluxTable &
         // with D = dH_eff/dL, H_real omega = M^2 D exactly (H_real = M s,
         // omega = M D / s), and omega = M D / s with s from the same square root
         const double D = x.ev[3][0] + x.od[3][0];
-        const double hw = (J.M * J.M) * D;
+        const double hw = J.M2 * D;
         double Tm, k4m;
         flux_m_factors((lane & 7) + 1, 4.0 * kPi * hw, hw, &Tm, &k4m);
         if (lane < 8) {

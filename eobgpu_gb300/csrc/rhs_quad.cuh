@@ -207,7 +207,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         od.dL = x.od[3][lane];
         const HamPart hp = comb_final_s(J, u, ev, od, x.hs[0][lane], x.hs[1][lane]);
         // 4 k^2 = 4 (m H_real omega)^2 of the m factors, H_real omega = M^2 D
-        const double k4m = flux_m_factor_k4(ql.md, (J.M * J.M) * D);
+        const double k4m = flux_m_factor_k4(ql.md, J.M2 * D);
         if (lane < 8) x.k4[lane] = k4m;
         const double omega = __shfl_sync(0xffffffffu, hp.dHdL, 0);
         const double omega_c = __shfl_sync(0xffffffffu, hp.dHdL, 1);
@@ -224,7 +224,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
     } else if (q == 1) {
         // m x / (1 - e^{-m x}), x = 4 pi H_real omega = 4 pi M^2 D
         // (H_real = M s, omega = M D / s)
-        const double Tm = flux_m_factor_T(ql.md, 4.0 * kPi * ((J.M * J.M) * D));
+        const double Tm = flux_m_factor_T(ql.md, 4.0 * kPi * (J.M2 * D));
         if (lane < 8) x.T[lane] = Tm;
     } else {
         // omega = M D / s at the state
@@ -246,7 +246,7 @@ __device__ __forceinline__ void eob_rhs_quad(const HamJets &J, const FluxTable &
         } else {
             // log v = log(omega) / 3, and S_even from H_real^2 = M^2 s^2
             // (no square root on that branch)
-            const double Se = fma(fma(J.M * J.M, s2, -1.0), t.inv2eta, 1.0);
+            const double Se = fma(fma(J.M2, s2, -1.0), t.inv2eta, 1.0);
             const double lv = eob_log(omega) * (1.0 / 3.0);
             const double elm = t.elog[(lane & 7) + 1] + lv;
             if (lane < 8) x.elm[lane] = elm;
