@@ -44,6 +44,14 @@ struct HamCoeffs {
     double q8c[3], q8h;
     // N_j(u) = sum_k (nc[j][k] + ncl[j][k] log r) u^k,  j = 0..4 (power of pr^2), k = 0..4
     double nc[5][5], ncl[5][5];
+    // the coefficients of the u-derivatives (k c_k) and the doubled
+    // constants, formed once per binary: the same products ham_eval formed
+    // at every call
+    struct Derived {
+        double ak0l6, ak0l5, ak0h, fa2, as6, as5, as4, dbl5, dbl4, dbh, bs4, bs3, two_ap2;
+        double q4c4, q4c3, q4c2, q4h, q6h, q6c3, q6c2, q8h, q8c2;
+        double nc02, nc03, nc04, nc12, nc13, four_n4, two_nu;
+    } d;
 };
 
 // m_1, m_2 as stored in the reference's additionalArgs (scaled to M = 1 by
@@ -213,6 +221,36 @@ EOB_HD void ham_coeffs_build(HamCoeffs *h, double m_1, double m_2, double chi_1,
         }
     h->nc[0][2] += c1 * X1 * g31 + c2 * X2 * g32;
     h->nc[0][4] += soc;
+    HamCoeffs::Derived &d = h->d;
+    d.ak0l6 = 6.0 * h->ak0l[6];
+    d.ak0l5 = 5.0 * h->ak0l[5];
+    d.ak0h = 6.5 * h->ak0h;
+    d.fa2 = 2.0 * h->fa2;
+    d.as6 = 6.0 * h->as6;
+    d.as5 = 5.0 * h->as5;
+    d.as4 = 4.0 * h->as4;
+    d.dbl5 = 5.0 * h->dbl[5];
+    d.dbl4 = 4.0 * h->dbl[4];
+    d.dbh = 5.5 * h->dbh;
+    d.bs4 = 4.0 * h->bs4;
+    d.bs3 = 3.0 * h->bs3;
+    d.two_ap2 = 2.0 * h->ap2;
+    d.q4c4 = 4.0 * h->q4c[4];
+    d.q4c3 = 3.0 * h->q4c[3];
+    d.q4c2 = 2.0 * h->q4c[2];
+    d.q4h = 4.5 * h->q4h;
+    d.q6h = 3.5 * h->q6h;
+    d.q6c3 = 3.0 * h->q6c[3];
+    d.q6c2 = 2.0 * h->q6c[2];
+    d.q8h = 2.5 * h->q8h;
+    d.q8c2 = 2.0 * h->q8c[2];
+    d.nc02 = 2.0 * h->nc[0][2];
+    d.nc03 = 3.0 * h->nc[0][3];
+    d.nc04 = 4.0 * h->nc[0][4];
+    d.nc12 = 2.0 * h->nc[1][2];
+    d.nc13 = 3.0 * h->nc[1][3];
+    d.four_n4 = 4.0 * h->nc[4][0];
+    d.two_nu = 2.0 * h->nu;
 }
 
 // ---------------------------------------------------------------------------

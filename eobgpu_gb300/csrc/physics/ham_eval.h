@@ -214,16 +214,16 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
     Jet ak0 = poly_jet<7>(h.ak0, u);
     {
         const double pl = u5 * fma(h.ak0l[6], u, h.ak0l[5]);
-        const double dpl = u4 * fma(6.0 * h.ak0l[6], u, 5.0 * h.ak0l[5]);
+        const double dpl = u4 * fma(h.d.ak0l6, u, h.d.ak0l5);
         const double hv = h.ak0h * u5 * u * su;
         ak0.v += fma(lr, pl, hv);
-        ak0.d += fma(lr, dpl, fma(6.5 * h.ak0h, u5 * su, -pl * r));
+        ak0.d += fma(lr, dpl, fma(h.d.ak0h, u5 * su, -pl * r));
     }
     const Jet aka = poly_jet<7>(h.aka, u);
     const Jet S = {ak0.v + aka.v, ak0.d + aka.d};
-    const Jet fa = {fma(fma(h.fa2, u, h.fa1), u, 1.0), fma(2.0 * h.fa2, u, h.fa1)};
+    const Jet fa = {fma(fma(h.fa2, u, h.fa1), u, 1.0), fma(h.d.fa2, u, h.fa1)};
     const Jet as = {1.0 + u4 * fma(fma(h.as6, u, h.as5), u, h.as4),
-                    u3 * fma(fma(6.0 * h.as6, u, 5.0 * h.as5), u, 4.0 * h.as4)};
+                    u3 * fma(fma(h.d.as6, u, h.d.as5), u, h.d.as4)};
     const double ap2 = h.ap2;
     const Jet dc = {1.0 + ap2 * u2 * (1.0 + 2.0 * u), ap2 * u * (2.0 + 6.0 * u)};
     const double idc = eob_rcp(dc.v);
@@ -236,16 +236,16 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
     Jet db = poly_jet<6>(h.db, u);
     {
         const double pl = u4 * fma(h.dbl[5], u, h.dbl[4]);
-        const double dpl = u3 * fma(5.0 * h.dbl[5], u, 4.0 * h.dbl[4]);
+        const double dpl = u3 * fma(h.d.dbl5, u, h.d.dbl4);
         const double hv = h.dbh * u5 * su;
         db.v += fma(lr, pl, hv);
-        db.d += fma(lr, dpl, fma(5.5 * h.dbh, u4 * su, -pl * r));
+        db.d += fma(lr, dpl, fma(h.d.dbh, u4 * su, -pl * r));
     }
     const double g = fma(h.kb, u, 1.0);
     const double ad = ak0.v * db.v;
     Jet bnp;
     bnp.v = ad * g + u3 * fma(h.bs4, u, h.bs3) - 1.0 + ap2 * u2;
-    bnp.d = (ak0.d * db.v + ak0.v * db.d) * g + ad * h.kb + u2 * fma(4.0 * h.bs4, u, 3.0 * h.bs3) + 2.0 * ap2 * u;
+    bnp.d = (ak0.d * db.v + ak0.v * db.d) * g + ad * h.kb + u2 * fma(h.d.bs4, u, h.d.bs3) + h.d.two_ap2 * u;
     // Bnpa = -(u^2 + 2 u^3) / Dc ;  c = u^2 (1 + apsq Bnpa)
     const double bnpa = -(u2 + 2.0 * u3) * idc;
     const double dbnpa = (-(2.0 * u + 6.0 * u2) - bnpa * dc.d) * idc;
@@ -254,12 +254,12 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
 
     // q4, q6, q8
     const Jet q4 = {u2 * fma(fma(h.q4c[4], u, h.q4c[3]), u, h.q4c[2]) + u4 * fma(h.q4l, lr, h.q4h * su),
-                    u * fma(fma(4.0 * h.q4c[4], u, 3.0 * h.q4c[3]), u, 2.0 * h.q4c[2]) +
-                        u3 * fma(h.q4l, 4.0 * lr - 1.0, 4.5 * h.q4h * su)};
+                    u * fma(fma(h.d.q4c4, u, h.d.q4c3), u, h.d.q4c2) +
+                        u3 * fma(h.q4l, 4.0 * lr - 1.0, h.d.q4h * su)};
     const Jet q6 = {u2 * fma(h.q6h * su + h.q6c[3], u, h.q6c[2]),
-                    u * fma(fma(3.5 * h.q6h, su, 3.0 * h.q6c[3]), u, 2.0 * h.q6c[2])};
+                    u * fma(fma(h.d.q6h, su, h.d.q6c3), u, h.d.q6c2)};
     const Jet q8 = {u * fma(h.q8h * su + h.q8c[2], u, h.q8c[1]),
-                    fma(fma(2.5 * h.q8h, su, 2.0 * h.q8c[2]), u, h.q8c[1])};
+                    fma(fma(h.d.q8h, su, h.d.q8c2), u, h.q8c[1])};
 
     const double p2 = pr * pr, L2 = L * L;
     const double qa = fma(p2, fma(p2, q8.v, q6.v), q4.v);
@@ -280,25 +280,25 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
     // odd part: N = sum_j p2^j N_j(u), N_j triangular in u (k <= 4 - j)
     const double(*nc)[5] = h.nc;
     const Jet n0 = {nc[0][0] + u * (nc[0][1] + u * (nc[0][2] + u * (nc[0][3] + u * nc[0][4]))) + h.ncl[0][4] * u4 * lr,
-                    nc[0][1] + u * (2.0 * nc[0][2] + u * (3.0 * nc[0][3] + u * 4.0 * nc[0][4])) +
+                    nc[0][1] + u * (h.d.nc02 + u * (h.d.nc03 + u * h.d.nc04)) +
                         h.ncl[0][4] * u3 * (4.0 * lr - 1.0)};
     const Jet n1 = {nc[1][0] + u * (nc[1][1] + u * (nc[1][2] + u * nc[1][3])) + h.ncl[1][3] * u3 * lr,
-                    nc[1][1] + u * (2.0 * nc[1][2] + u * 3.0 * nc[1][3]) + h.ncl[1][3] * u2 * (3.0 * lr - 1.0)};
+                    nc[1][1] + u * (h.d.nc12 + u * 3.0 * nc[1][3]) + h.ncl[1][3] * u2 * (3.0 * lr - 1.0)};
     const Jet n2 = {nc[2][0] + u * (nc[2][1] + u * nc[2][2]), nc[2][1] + 2.0 * u * nc[2][2]};
     const Jet n3 = {nc[3][0] + u * nc[3][1], nc[3][1]};
     const double n4 = nc[4][0];
     const double Nv = n0.v + p2 * (n1.v + p2 * (n2.v + p2 * (n3.v + p2 * n4)));
     const double Nu = n0.d + p2 * (n1.d + p2 * (n2.d + p2 * n3.d));
-    const double Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * 4.0 * n4));
+    const double Np = n1.v + p2 * (2.0 * n2.v + p2 * (3.0 * n3.v + p2 * h.d.four_n4));
     const double u3i = u3 * idc;
     const double hodd = L * u3i * Nv;
     const double hodd_u = L * idc * (3.0 * u2 * Nv + u3 * Nu - u3 * Nv * idc * dc.d);
-    const double hodd_p = L * u3i * Np * 2.0 * pr;
+    const double hodd_p = (L * u3i * Np) * (2.0 * pr);  // the same bits: the products by 2 are exact
     const double hodd_L = u3i * Nv;
 
     const double heff = heven + hodd;
     const double nu = h.nu, M = h.M;
-    const double s2 = fma(2.0 * nu, heff - 1.0, 1.0);
+    const double s2 = fma(h.d.two_nu, heff - 1.0, 1.0);
     const double rs = eob_rsqrt(s2);
     const double s = s2 * rs;
     const double H = M * s / nu;
@@ -314,7 +314,7 @@ EOB_HD void ham_eval(const HamCoeffs &h, double r, double pr, double L, HamEval 
     const double AW0 = A.v * W0;
     const double r0 = eob_rsqrt(AW0);
     const double hodd0 = L * u3i * n0.v;
-    const double rs0 = eob_rsqrt(fma(2.0 * nu, fma(AW0, r0, hodd0) - 1.0, 1.0));
+    const double rs0 = eob_rsqrt(fma(h.d.two_nu, fma(AW0, r0, hodd0) - 1.0, 1.0));
     out->omega_c = (M * rs0) * fma(A.v * L * cu.v, r0, u3i * n0.v);
 }
 

@@ -116,7 +116,7 @@ int eob_synth_strain(void *workspace, size_t workspace_bytes, int max_batch, int
  * memory pool, a plugin host without allocator access, or a process that must
  * not call cudaMalloc while other work is in flight passes only its inputs
  * and outputs; the scratch is a fixed __device__ array of
- * eob_noalloc_scratch_bytes() bytes (13 585 152 bytes, 13.6 MB) that every
+ * eob_noalloc_scratch_bytes() bytes (13 588 736 bytes, 13.6 MB) that every
  * GPU loading the library keeps until exit.  Limits: B <= 16 binaries, K = 1 mode,
  * N <= 8192 samples, at most 4096 trajectory rows per binary (longer
  * trajectories end with EOB_ST_MAXSTEP); larger calls return EOB_E_ARG.
